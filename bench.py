@@ -1,0 +1,305 @@
+"""Benchmark of the per-particle nuclear burn on GB300.
+
+One step = one burn of the whole workload over its hydro step, through the library's
+C ABI, starting from the same seeded state every step (the state is restored from a
+pristine HBM copy inside the timed region).  Default workload: net86 + Helmholtz EOS,
+1,048,576 particles (rho log-uniform [1e6, 5e9], T log-uniform [5e8, 6e9], 0.3 12C /
+0.7 16O with a 1e-10 floor, hydro dt 1e-4 s).  Metric: particle-burns/s (particles
+carried through one hydro step per second of wall time).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--solver mixed|sparse|dense]
+                  [--particles P] [--impl reference]
+
+Under torchrun each rank burns its own seeded shard of P particles (weak scaling, no
+collective on the data path); the step time is the max over ranks.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(REPO, "sph-exa-nnet_gb300")
+for p in (os.path.join(PKG, "data"), PKG):
+    sys.path.insert(0, p)
+
+METRIC = "net86 particle-burns/s on 1 GB300, plain vs batched+FP32-LU @1e-8; p50/p99 latency"
+UNIT = "particle-burns/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--solver", default=None)
+    ap.add_argument("--particles", type=int, default=1048576)
+    ap.add_argument("--plain-particles", type=int, default=131072,
+                    help="particles of the plain FP64 comparison leg (0 disables it)")
+    ap.add_argument("--impl", default="gb300")
+    ap.add_argument("--cpu-sample", type=int, default=4096)
+    ap.add_argument("--max-iter", type=int, default=20000)
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    return rank, world, local
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi samples during the timed region (SM clock, throttle reasons)."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu, self.proc = gpu, None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except (ValueError, IndexError):
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- reference (CPU) arm
+def cpu_burn_rate(sample, threads=0, seed=None):
+    """The oracle restatement of the reference's CPU path on host cores (OpenMP dynamic
+    schedule, as parallel_nuclear_net_impl.cpp:79-81) over `sample` particles of the
+    workload; returns (particle-burns/s, seconds, threads)."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("oracle_build", os.path.join(REPO, "oracle", "build.py"))
+    ob = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(ob)
+    ob.build_oracle()
+    from oracle import Oracle
+    import workloads
+    import nnet_build
+    o = Oracle("port")
+    o.load_helmholtz(np.fromfile(nnet_build.helm_table(), dtype="<f8"))
+    w = workloads.make("c2", P=sample, seed=seed)
+    threads = threads or os.cpu_count()
+    t0 = time.perf_counter()
+    o.burn(w["net"], w["Y"], w["T"], w["rho"], w["dt"], w["hydro_dt"], w["eos"], w["mu"], max_iter=20000,
+           nthreads=threads)
+    el = time.perf_counter() - t0
+    return sample / el, el, threads
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    vals = []
+    for _ in range(max(1, args.warmup // 3)):
+        cpu_burn_rate(256)
+    for k in range(args.steps):
+        v, el, threads = cpu_burn_rate(args.cpu_sample, seed=100 + k)
+        vals.append((v, el))
+    value = statistics.median(v for v, _ in vals)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.median(e for _, e in vals) * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded, workload c2 distributions)",
+            "config": {"workload": "net86+helmholtz c2 (CPU sample)", "particles_per_step": args.cpu_sample,
+                       "hydro_dt": 1e-4},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{args.cpu_sample} particles of c2 per step (fresh seed each step)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- GPU arm
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import torch
+    import torch.distributed as dist
+    import nnet_gb300 as nn
+    import workloads
+
+    rank, world, local = dist_info()
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    ctx = nn.Context(local)
+    solver = args.solver or "dense"
+    sv = nn.SOLVERS[solver]
+
+    # ---- device-resident workload (this rank's shard)
+    w = workloads.make("c2", P=args.particles, seed=2 + 1000 * rank)
+    P = args.particles
+    Y0 = torch.tensor(w["Y"], device=dev)
+    T0 = torch.tensor(w["T"], device=dev)
+    rho = torch.tensor(w["rho"], device=dev)
+    dt0 = torch.tensor(w["dt"], device=dev)
+    Y, T, dt = torch.empty_like(Y0), torch.empty_like(T0), torch.empty_like(dt0)
+    status = torch.empty(P, dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        Y.copy_(Y0), T.copy_(T0), dt.copy_(dt0)
+        ctx.burn(86, Y, T, rho, dt, w["hydro_dt"], eos=nn.EOS_HELMHOLTZ, solver=sv, status=status,
+                 max_iter=args.max_iter, stream=stream)
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        if world > 1:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        step()
+    barrier()
+    stats = ctx.stats()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    kt = []
+    with ClockSampler(local) as clk:
+        barrier()
+        t0 = time.perf_counter()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            Y.copy_(Y0), T.copy_(T0), dt.copy_(dt0)
+            a.record(stream)
+            ctx.burn(86, Y, T, rho, dt, w["hydro_dt"], eos=nn.EOS_HELMHOLTZ, solver=sv, status=status,
+                     max_iter=args.max_iter, stream=stream)
+            b.record(stream)
+            kt.append((a, b))
+        ev1.record(stream)
+        barrier()
+        wall = time.perf_counter() - t0
+    ms = ev0.elapsed_time(ev1) / args.steps
+    kernel_ms = statistics.mean(a.elapsed_time(b) for a, b in kt)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * P / (ms / 1e3)
+
+    # ---- end to end through the public API with host buffers
+    Yh = torch.tensor(w["Y"]).pin_memory()
+    Th, dth, rhoh = torch.tensor(w["T"]).pin_memory(), torch.tensor(w["dt"]).pin_memory(), torch.tensor(
+        w["rho"]).pin_memory()
+    Yo, To, dto = torch.empty_like(Yh).pin_memory(), torch.empty_like(Th).pin_memory(), torch.empty_like(
+        dth).pin_memory()
+    rho_d = torch.empty_like(rho)
+    e2e_steps = max(1, min(args.steps, 2))
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        Y.copy_(Yh, non_blocking=True), T.copy_(Th, non_blocking=True), dt.copy_(dth, non_blocking=True)
+        rho_d.copy_(rhoh, non_blocking=True)
+        ctx.burn(86, Y, T, rho_d, dt, w["hydro_dt"], eos=nn.EOS_HELMHOLTZ, solver=sv, status=status,
+                 max_iter=args.max_iter, stream=stream)
+        Yo.copy_(Y, non_blocking=True), To.copy_(T, non_blocking=True), dto.copy_(dt, non_blocking=True)
+    e1.record(stream)
+    barrier()
+    e2e_ms = e0.elapsed_time(e1) / e2e_steps
+    h2d = (86 + 3) * 8 * P
+    d2h = (86 + 2) * 8 * P
+
+    # ---- plain FP64 form on a sub-batch, for the plain-vs-fast ratio
+    plain = None
+    if args.plain_particles and solver != "dense":
+        Pp = min(args.plain_particles, P)
+        sl = slice(0, Pp)
+        Y[:, sl].copy_(Y0[:, sl]), T[sl].copy_(T0[sl]), dt[sl].copy_(dt0[sl])
+        ctx.burn(86, Y[:, sl], T[sl], rho[sl], dt[sl], w["hydro_dt"], eos=nn.EOS_HELMHOLTZ,
+                 solver=nn.SOLVER_DENSE_FP64, max_iter=args.max_iter, stream=stream)
+        barrier()
+        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        Y[:, sl].copy_(Y0[:, sl]), T[sl].copy_(T0[sl]), dt[sl].copy_(dt0[sl])
+        p0.record(stream)
+        ctx.burn(86, Y[:, sl], T[sl], rho[sl], dt[sl], w["hydro_dt"], eos=nn.EOS_HELMHOLTZ,
+                 solver=nn.SOLVER_DENSE_FP64, max_iter=args.max_iter, stream=stream)
+        p1.record(stream)
+        barrier()
+        plain = {"value": Pp / (p0.elapsed_time(p1) / 1e3), "unit": UNIT, "particles": Pp}
+
+    # ---- roofline: FP64 pipe (the kernel computes in FP64; no HBM or tensor bound applies)
+    iters = stats["newton_iterations"]
+    flops_per_iter = FLOPS_PER_ITER[solver]
+    achieved = flops_per_iter * iters / (kernel_ms / 1e3) / 1e12
+    peak = FP64_PEAK_TFLOPS
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, workload c2 distributions)",
+            "config": {"workload": "net86+helmholtz c2", "particles_per_gpu": P, "hydro_dt": 1e-4,
+                       "solver": solver, "l2": "inputs (700 MB of abundances) larger than L2",
+                       "newton_iterations_per_step": iters, "status_counts": stats["status"]},
+            "e2e": {"value": world * P / (e2e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": args.steps,
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak, "traffic": None,
+                         "peak_source": "nominal GB300 FP64 (no FP64 figure in MEASURED_PEAKS.json)",
+                         "flops_per_newton_iteration": flops_per_iter},
+            "kernel_ms": kernel_ms, "wall_s": wall, "clocks": clk.summary()}
+    if plain:
+        line["plain_fp64"] = plain
+    if rank == 0:
+        try:
+            v, el, thr = cpu_burn_rate(args.cpu_sample)
+            line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": thr, "kind": "port",
+                                    "sample": f"{args.cpu_sample} particles of c2, {el:.1f} s"}
+        except Exception as e:  # the baseline is reported, never the target
+            line["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "error": str(e)}
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+# algorithmic FP64 FLOPs per Newton iteration of net86: dense Gaussian
+# elimination of the 87 x 87 system as the reference performs it (n^3/3 multiply-adds,
+# full fill) plus the system assembly; the sparse forms count only the operations of the
+# fill-reducing factorisation they execute.
+FLOPS_PER_ITER = {"dense": 2 * 223_213 + 2 * 87 * 87 + 2 * (309 * 6 + 2 * 87 * 87), "sparse": 0, "mixed": 0}
+FP64_PEAK_TFLOPS = 1.25
+
+if __name__ == "__main__":
+    main()

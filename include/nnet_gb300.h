@@ -1,0 +1,153 @@
+/*
+ * nnet_gb300 — C ABI of the GB300 (sm_103a) nuclear-burn library.
+ *
+ * Drop-in replacement for the GPU side of SPH-EXA-nnet's per-particle burn path.  All
+ * entry points take plain pointers and sizes; device arrays are caller-owned and stay
+ * in place (Y, T and dt are updated in place, as in the reference).  Calls that take a
+ * stream are asynchronous with respect to the host unless stated otherwise.
+ *
+ * Reference interfaces replaced (file:line in SPH-EXA-nnet):
+ *   nnet::parallel::computeNuclearReactions<use_gpu=true>
+ *                       include/nnet/parallel/parallel_nuclear_net.hpp:86-142
+ *   nnet::parallel::cudaComputeNuclearReactions
+ *                       include/nnet/parallel/CUDA/parallel_nuclear_net.cuh:70-75, .cu:115-163
+ *   nnet::parallel::computeHelmEOS<use_gpu=true> / cudaComputeHelmholtz
+ *                       include/nnet/parallel/parallel_nuclear_net.hpp:191-231,
+ *                       include/nnet/parallel/CUDA/parallel_nuclear_net.cuh:77-79, .cu:216-226
+ *   helmholtz::constants::readCPUTable / copyTableToGPU
+ *                       include/nnet/parameterization/eos/helmholtz.cpp:89-218
+ *   net87::electrons::constants::copyTableToGPU, nnet::moveToGpu(ReactionList)
+ *                       include/nnet/parameterization/net87/net87.cpp:89-99,
+ *                       include/nnet/CUDA/nuclear_net.cuh:61-72
+ */
+#ifndef NNET_GB300_H
+#define NNET_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NNET_MAX_SPECIES 87
+
+/* Return codes of every entry point. */
+enum nnet_error
+{
+    NNET_SUCCESS         = 0,
+    NNET_ERR_INVALID     = -1, /* bad argument (null pointer, unknown network, size) */
+    NNET_ERR_CUDA        = -2, /* a CUDA runtime call failed; see nnet_last_error_message */
+    NNET_ERR_NO_TABLE    = -3, /* Helmholtz EOS requested before a table was loaded */
+    NNET_ERR_TOO_LARGE   = -4, /* request exceeds a fixed capacity */
+    NNET_ERR_FILE        = -5, /* table file missing or malformed */
+};
+
+/* Per-particle outcome written to nnet_burn_args.status (int32 per particle). */
+enum nnet_particle_status
+{
+    NNET_PARTICLE_OK       = 0, /* burned to hydro_dt */
+    NNET_PARTICLE_SKIPPED  = 1, /* rho <= 1e5 or T <= 1e8: left untouched (parallel_nuclear_net_impl.cpp:83) */
+    NNET_PARTICLE_LIVELOCK = 2, /* the substep loop reached a bit-exact fixed point: a rejected attempt
+                                   left dt unchanged, so the reference would retry it forever
+                                   (nuclear_net.hpp:745-748 with :899-904); state is that of the
+                                   last accepted substep */
+    NNET_PARTICLE_MAXITER  = 3, /* Newton-iteration budget exhausted */
+    NNET_PARTICLE_ZERO_DT  = 4, /* timestep underflowed to 0 (the reference throws, nuclear_net.hpp:533-549) */
+};
+
+enum nnet_network
+{
+    NNET_NET14 = 14, /* 14-isotope alpha chain, 29 reactions  (net14.hpp:69-134) */
+    NNET_NET86 = 86, /* 86 isotopes, 309 reactions              (net86.hpp:95-192) */
+    NNET_NET87 = 87, /* net86 + electrons, 311 reactions        (net87.hpp:88-98) */
+};
+
+enum nnet_eos
+{
+    NNET_EOS_IDEAL_GAS = 0, /* IdealGasFunctor(mu)             (ideal_gas.hpp:46-83) */
+    NNET_EOS_HELMHOLTZ = 1, /* HelmholtzFunctor(Z of network)  (helmholtz.hpp:150-226) */
+};
+
+/* Linear-solver form of the Newton step. */
+enum nnet_solver
+{
+    NNET_SOLVER_DENSE_FP64  = 0, /* plain form: dense Gaussian elimination in the reference's
+                                    operation order (eigen.hpp:155-198), one thread per particle */
+    NNET_SOLVER_SPARSE_FP64 = 1, /* fill-reducing sparse LU in FP64 */
+    NNET_SOLVER_MIXED       = 2, /* sparse LU factored in FP32, FP64 residual, iterative refinement */
+};
+
+typedef struct nnet_context* nnet_handle;
+
+/* Burn statistics accumulated over one nnet_burn call (device-side counters). */
+typedef struct
+{
+    unsigned long long newton_iterations;
+    unsigned long long substeps;
+    unsigned long long status_count[5]; /* indexed by nnet_particle_status */
+} nnet_stats;
+
+/* Arguments of nnet_burn.  All arrays are DEVICE pointers of num_particles entries. */
+typedef struct
+{
+    int           network;      /* nnet_network */
+    int           eos;          /* nnet_eos */
+    double        ideal_gas_mu; /* mean molecular weight for NNET_EOS_IDEAL_GAS */
+    int           solver;       /* nnet_solver */
+    size_t        num_particles;
+    double* const* Y;           /* host array of `network` device pointers, Y[species][particle]
+                                   (the reference's per-species field vectors) */
+    double*       T;            /* temperature, in/out */
+    const double* rho;          /* density at the end of the hydro step */
+    const double* rho_m1;       /* density at the previous step (may be NULL) */
+    double*       dt;           /* carried nuclear timestep, in/out */
+    double        hydro_dt;     /* integration time of this call */
+    double        previous_dt;  /* previous hydro step, for drho/dt */
+    int           use_drhodt;   /* drho/dt = (rho - rho_m1)/previous_dt where rho_m1 != 0,
+                                   as the CUDA driver does (parallel_nuclear_net.cu:80-82) */
+    long long     max_newton_iterations; /* per particle; <= 0 selects 100000 */
+    int32_t*      status;       /* optional, nnet_particle_status per particle */
+    int32_t*      substeps;     /* optional, accepted substeps per particle */
+    int32_t*      iterations;   /* optional, Newton iterations per particle */
+} nnet_burn_args;
+
+/* Create a context on `device` (network tables uploaded, no Helmholtz table yet). */
+int nnet_create(int device, nnet_handle* out);
+/* Release every device buffer held by the context. */
+int nnet_destroy(nnet_handle h);
+
+/* Load the Helmholtz free-energy table from host memory: 21 arrays of 541 x 201 doubles in
+ * the reference's quantity order f fd ft fdd ftt fdt fddt fdtt fddtt dpdf dpdfd dpdft
+ * dpdfdt ef efd eft efdt xf xfd xft xfdt, each row-major [density][temperature].
+ * Synchronous.  Replaces readCPUTable + copyTableToGPU (helmholtz.cpp:89-218). */
+int nnet_load_helmholtz_table(nnet_handle h, const double* table);
+/* Same, parsing the reference's text layout helm_table.dat (helmholtz.cpp:100-137); an
+ * optional STR( ... ) wrapper is accepted. */
+int nnet_load_helmholtz_table_file(nnet_handle h, const char* path);
+
+/* Burn num_particles particles over hydro_dt on `stream` (a cudaStream_t, 0 = legacy
+ * default stream).  Asynchronous; the per-call statistics become readable with
+ * nnet_get_stats after the stream has reached this point. */
+int nnet_burn(nnet_handle h, const nnet_burn_args* args, void* stream);
+/* Copy the statistics of the last nnet_burn issued on this handle (synchronises the
+ * handle's internal stream). */
+int nnet_get_stats(nnet_handle h, nnet_stats* out);
+
+/* Post-burn Helmholtz EOS over a batch (computeHelmEOS, parallel_nuclear_net.hpp:191-231):
+ * writes u, cv, p, c, dpdT per particle.  Z has `num_species` host doubles; Y is a host
+ * array of device pointers.  Asynchronous on `stream`. */
+int nnet_helmholtz_eos(nnet_handle h, size_t num_particles, int num_species, const double* Z,
+                       const double* T, const double* rho, double* const* Y, double* u, double* cv,
+                       double* p, double* c, double* dpdT, void* stream);
+
+/* Number of species / reactions of a network, 0 on success. */
+int nnet_network_info(int network, int* num_species, int* num_reactions);
+/* Human-readable description of the last error on this thread. */
+const char* nnet_last_error_message(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NNET_GB300_H */

@@ -1,0 +1,397 @@
+// C ABI of the GB300 burn library (include/nnet_gb300.h): context, table upload, burn
+// dispatch and the post-burn Helmholtz EOS.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "physics.cuh"
+#include "launch.hpp"
+
+using namespace nnet_gb300;
+
+namespace
+{
+thread_local std::string g_lastError;
+
+int fail(int code, const std::string& msg)
+{
+    g_lastError = msg;
+    return code;
+}
+
+#define NNET_CUDA(call)                                                                                               \
+    do                                                                                                                \
+    {                                                                                                                 \
+        cudaError_t e_ = (call);                                                                                      \
+        if (e_ != cudaSuccess)                                                                                        \
+            return fail(NNET_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));                           \
+    } while (0)
+
+// one device allocation per network holding every table of NetView
+struct NetBuffer
+{
+    void*   mem = nullptr;
+    NetView view{};
+};
+
+int uploadNetwork(int net, NetBuffer& b)
+{
+    const int N = net, R = net == 14 ? NET14_NUM_REACTIONS : net == 86 ? NET86_NUM_REACTIONS : NET87_NUM_REACTIONS;
+    const int *rbeg, *rspec, *rcnt, *pbeg, *pspec, *pcnt;
+    const double *BE, *Z, *fit, *q, *choose;
+    int nfit, nq, nchoose;
+    if (net == 14)
+    {
+        rbeg = net14_reactant_begin, rspec = net14_reactant_species, rcnt = net14_reactant_count;
+        pbeg = net14_product_begin, pspec = net14_product_species, pcnt = net14_product_count;
+        BE = net14_BE, Z = net14_Z, fit = net14_fit, q = net14_q, choose = net14_choose;
+        nfit = 80, nq = 10, nchoose = 264;
+    }
+    else
+    {
+        if (net == 86)
+        {
+            rbeg = net86_reactant_begin, rspec = net86_reactant_species, rcnt = net86_reactant_count;
+            pbeg = net86_product_begin, pspec = net86_product_species, pcnt = net86_product_count;
+            BE = net86_BE;
+        }
+        else
+        {
+            rbeg = net87_reactant_begin, rspec = net87_reactant_species, rcnt = net87_reactant_count;
+            pbeg = net87_product_begin, pspec = net87_product_species, pcnt = net87_product_count;
+            BE = net87_BE;
+        }
+        Z = net86_Z, fit = net86_fit, q = net86_q, choose = net86_choose;
+        nfit = 1200, nq = 150, nchoose = 1944;
+    }
+    const int nr = rbeg[R], np = pbeg[R];
+    // doubles: BE, Z, z53 (N each, Z padded to 87), fit, q, choose, electron tables
+    std::vector<double> d;
+    auto putd = [&](const double* src, size_t n) {
+        size_t o = d.size();
+        d.insert(d.end(), src, src + n);
+        return o;
+    };
+    std::vector<double> z53(N, 0.);
+    for (int i = 0; i < N && i < (net == 14 ? 14 : 86); ++i)
+        z53[i] = std::pow(Z[i], 5. / 3.); // host libm, as the reference's per-call pow(Z, 5/3)
+    const size_t oBE = putd(BE, N), oZ = putd(Z, net == 14 ? 14 : 87), oZ53 = putd(z53.data(), N);
+    const size_t oFit = putd(fit, nfit), oQ = putd(q, nq), oCh = putd(choose, nchoose);
+    const size_t oLT = putd(net87_electron_log_temp, NET87_ELECTRON_NTEMP);
+    const size_t oLR = putd(net87_electron_log_rho, NET87_ELECTRON_NRHO);
+    const size_t oER = putd(net87_electron_rate, (size_t)NET87_ELECTRON_NTEMP * NET87_ELECTRON_NRHO * NET87_ELECTRON_NC);
+    std::vector<int> ii;
+    auto puti = [&](const int* src, size_t n) {
+        size_t o = ii.size();
+        ii.insert(ii.end(), src, src + n);
+        return o;
+    };
+    const size_t oRb = puti(rbeg, R + 1), oRs = puti(rspec, nr), oRc = puti(rcnt, nr);
+    const size_t oPb = puti(pbeg, R + 1), oPs = puti(pspec, np), oPc = puti(pcnt, np);
+    const size_t oMr = puti(net86_main_reactant, 157), oSr = puti(net86_secondary_reactant, 157),
+                 oMp = puti(net86_main_product, 157);
+    const size_t bytesD = d.size() * sizeof(double), bytes = bytesD + ii.size() * sizeof(int);
+    NNET_CUDA(cudaMalloc(&b.mem, bytes));
+    NNET_CUDA(cudaMemcpy(b.mem, d.data(), bytesD, cudaMemcpyHostToDevice));
+    NNET_CUDA(cudaMemcpy((char*)b.mem + bytesD, ii.data(), ii.size() * sizeof(int), cudaMemcpyHostToDevice));
+    const double* D = (const double*)b.mem;
+    const int*    I = (const int*)((const char*)b.mem + bytesD);
+    NetView&      v = b.view;
+    v.net = net, v.nspec = N, v.nreact = R;
+    v.rbeg = I + oRb, v.rspec = I + oRs, v.rcnt = I + oRc, v.pbeg = I + oPb, v.pspec = I + oPs, v.pcnt = I + oPc;
+    v.BE = D + oBE, v.Z = D + oZ, v.z53 = D + oZ53, v.fit = D + oFit, v.q = D + oQ, v.choose = D + oCh;
+    v.mainReactant = I + oMr, v.secondaryReactant = I + oSr, v.mainProduct = I + oMp;
+    v.eLogT = D + oLT, v.eLogRho = D + oLR, v.eRate = D + oER;
+    return NNET_SUCCESS;
+}
+
+int netIndex(int net) { return net == 14 ? 0 : net == 86 ? 1 : net == 87 ? 2 : -1; }
+
+// post-burn EOS: one thread per particle (parallel_nuclear_net.cu:184-210)
+struct EosParams
+{
+    size_t        P;
+    int           dim;
+    double        Z[NNET_MAX_SPECIES];
+    const double* Y[NNET_MAX_SPECIES];
+    const double *T, *rho;
+    double *      u, *cv, *p, *c, *dpdT;
+};
+
+__global__ void helmholtzEosKernel(EosParams ep, HelmView hv)
+{
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < ep.P; i += (size_t)gridDim.x * blockDim.x)
+    {
+        double abar = 0, zbar = 0;
+        for (int j = 0; j < ep.dim; ++j)
+        {
+            const double y = ep.Y[j][i];
+            abar += y;
+            zbar += y * ep.Z[j];
+        }
+        const EosResult r = helmholtzEos(hv, abar, zbar, ep.T[i], ep.rho[i]);
+        ep.u[i] = r.u, ep.cv[i] = r.cv, ep.p[i] = r.p, ep.c[i] = r.c, ep.dpdT[i] = r.dpdT;
+    }
+}
+} // namespace
+
+struct nnet_context
+{
+    int                 device = 0, numSMs = 0;
+    NetBuffer           nets[3];
+    void*               helmMem    = nullptr;
+    HelmView            helm{};
+    bool                helmLoaded = false;
+    double*             scratch    = nullptr;
+    size_t              scratchDoubles = 0;
+    unsigned long long* counters   = nullptr; // [0] queue, [1..7] stats
+    cudaStream_t        lastStream = nullptr;
+};
+
+extern "C" {
+
+const char* nnet_last_error_message(void) { return g_lastError.c_str(); }
+
+int nnet_network_info(int network, int* num_species, int* num_reactions)
+{
+    if (netIndex(network) < 0) return fail(NNET_ERR_INVALID, "unknown network");
+    if (num_species) *num_species = network;
+    if (num_reactions)
+        *num_reactions = network == 14 ? NET14_NUM_REACTIONS : network == 86 ? NET86_NUM_REACTIONS : NET87_NUM_REACTIONS;
+    return NNET_SUCCESS;
+}
+
+int nnet_create(int device, nnet_handle* out)
+{
+    if (!out) return fail(NNET_ERR_INVALID, "null handle pointer");
+    NNET_CUDA(cudaSetDevice(device));
+    nnet_context* h = new nnet_context;
+    h->device       = device;
+    cudaDeviceGetAttribute(&h->numSMs, cudaDevAttrMultiProcessorCount, device);
+    const int nets[3] = {14, 86, 87};
+    for (int k = 0; k < 3; ++k)
+    {
+        int rc = uploadNetwork(nets[k], h->nets[k]);
+        if (rc)
+        {
+            nnet_destroy(h);
+            return rc;
+        }
+    }
+    if (cudaMalloc(&h->counters, 8 * sizeof(unsigned long long)) != cudaSuccess)
+    {
+        nnet_destroy(h);
+        return fail(NNET_ERR_CUDA, "cudaMalloc counters");
+    }
+    cudaMemset(h->counters, 0, 8 * sizeof(unsigned long long));
+    *out = h;
+    return NNET_SUCCESS;
+}
+
+int nnet_destroy(nnet_handle h)
+{
+    if (!h) return NNET_SUCCESS;
+    cudaSetDevice(h->device);
+    cudaDeviceSynchronize();
+    for (auto& n : h->nets)
+        if (n.mem) cudaFree(n.mem);
+    if (h->helmMem) cudaFree(h->helmMem);
+    if (h->scratch) cudaFree(h->scratch);
+    if (h->counters) cudaFree(h->counters);
+    delete h;
+    return NNET_SUCCESS;
+}
+
+int nnet_load_helmholtz_table(nnet_handle h, const double* table)
+{
+    if (!h || !table) return fail(NNET_ERR_INVALID, "null argument");
+    NNET_CUDA(cudaSetDevice(h->device));
+    constexpr int I = HELM_IMAX, J = HELM_JMAX, C = HELM_CELL;
+    // cell layout: f ft ftt fd fdd fdt fddt fdtt fddtt dpdf dpdft dpdfd dpdfdt (reference
+    // table indices 0 2 4 1 3 5 6 7 8 9 11 10 12)
+    static const int src[13] = {0, 2, 4, 1, 3, 5, 6, 7, 8, 9, 11, 10, 12};
+    const size_t     ncell   = (size_t)I * J * C;
+    std::vector<double> host(ncell + 9 * (size_t)I, 0.);
+    for (int i = 0; i < I; ++i)
+        for (int j = 0; j < J; ++j)
+            for (int q = 0; q < 13; ++q)
+                host[((size_t)i * J + j) * C + q] = table[((size_t)src[q] * I + i) * J + j];
+    // grid and spacing arrays exactly as the reference computes them (helmholtz.cpp:101-169)
+    const double tlo = 3., thi = 13., tstp = (thi - tlo) / (double)(J - 1);
+    const double dlo = -12., dhi = 15., dstp = (dhi - dlo) / (double)(I - 1);
+    double*      g = host.data() + ncell; // 9 arrays of I doubles
+    double *d = g, *ddS = g + I, *dd2S = g + 2 * I, *ddiS = g + 3 * I, *t = g + 4 * I, *dtS = g + 5 * I,
+           *dt2S = g + 6 * I, *dtiS = g + 7 * I, *dt2iS = g + 8 * I;
+    for (int i = 0; i < I; ++i)
+        d[i] = std::pow((double)10., dlo + i * dstp);
+    for (int j = 0; j < J; ++j)
+        t[j] = std::pow((double)10., tlo + j * tstp);
+    for (int j = 0; j < J - 1; ++j)
+    {
+        const double dth = t[j + 1] - t[j], dt2 = dth * dth, dti = 1. / dth;
+        dtS[j] = dth, dt2S[j] = dt2, dtiS[j] = dti, dt2iS[j] = 1. / dt2;
+    }
+    for (int i = 0; i < I - 1; ++i)
+    {
+        const double dd = d[i + 1] - d[i], dd2 = dd * dd;
+        ddS[i] = dd, dd2S[i] = dd2, ddiS[i] = 1. / dd;
+    }
+    if (!h->helmMem) NNET_CUDA(cudaMalloc(&h->helmMem, host.size() * sizeof(double)));
+    NNET_CUDA(cudaMemcpy(h->helmMem, host.data(), host.size() * sizeof(double), cudaMemcpyHostToDevice));
+    const double* D = (const double*)h->helmMem;
+    const double* G = D + ncell;
+    h->helm         = {D, G, G + I, G + 2 * I, G + 3 * I, G + 4 * I, G + 5 * I, G + 6 * I, G + 7 * I, G + 8 * I};
+    h->helmLoaded   = true;
+    return NNET_SUCCESS;
+}
+
+int nnet_load_helmholtz_table_file(nnet_handle h, const char* path)
+{
+    if (!h || !path) return fail(NNET_ERR_INVALID, "null argument");
+    std::ifstream f(path);
+    if (!f) return fail(NNET_ERR_FILE, std::string("cannot open ") + path);
+    std::stringstream ss;
+    ss << f.rdbuf();
+    std::string s = ss.str();
+    // accept the STR( ... ) wrapper the reference #includes (helmholtz.cpp:92-94)
+    size_t a = s.find("STR(");
+    if (a != std::string::npos)
+    {
+        s        = s.substr(a + 4);
+        size_t b = s.rfind(')');
+        if (b != std::string::npos) s = s.substr(0, b);
+    }
+    constexpr int       I = HELM_IMAX, J = HELM_JMAX;
+    std::vector<double> tab((size_t)21 * I * J);
+    const char*         c   = s.c_str();
+    char*               end = nullptr;
+    auto                next = [&](double& v) {
+        v = std::strtod(c, &end);
+        if (end == c) return false;
+        c = end;
+        return true;
+    };
+    auto at = [&](int k, int i, int j) -> double& { return tab[((size_t)k * I + i) * J + j]; };
+    // f-block: 9 quantities per (j, i); then three 4-quantity blocks (helmholtz.cpp:106-137)
+    for (int j = 0; j < J; ++j)
+        for (int i = 0; i < I; ++i)
+            for (int k = 0; k < 9; ++k)
+                if (!next(at(k, i, j))) return fail(NNET_ERR_FILE, "truncated Helmholtz table");
+    for (int blk = 0; blk < 3; ++blk)
+        for (int j = 0; j < J; ++j)
+            for (int i = 0; i < I; ++i)
+                for (int k = 0; k < 4; ++k)
+                    if (!next(at(9 + 4 * blk + k, i, j))) return fail(NNET_ERR_FILE, "truncated Helmholtz table");
+    return nnet_load_helmholtz_table(h, tab.data());
+}
+
+int nnet_burn(nnet_handle h, const nnet_burn_args* a, void* stream)
+{
+    if (!h || !a) return fail(NNET_ERR_INVALID, "null argument");
+    const int ni = netIndex(a->network);
+    if (ni < 0) return fail(NNET_ERR_INVALID, "unknown network");
+    if (a->eos != NNET_EOS_IDEAL_GAS && a->eos != NNET_EOS_HELMHOLTZ) return fail(NNET_ERR_INVALID, "unknown eos");
+    if (a->eos == NNET_EOS_HELMHOLTZ && !h->helmLoaded)
+        return fail(NNET_ERR_NO_TABLE, "Helmholtz EOS requested before nnet_load_helmholtz_table");
+    if (a->eos == NNET_EOS_IDEAL_GAS && !(a->ideal_gas_mu > 0)) return fail(NNET_ERR_INVALID, "ideal_gas_mu must be > 0");
+    if (a->num_particles == 0) return NNET_SUCCESS;
+    if (!a->Y || !a->T || !a->rho || !a->dt) return fail(NNET_ERR_INVALID, "null particle array");
+    if (!(a->hydro_dt > 0)) return fail(NNET_ERR_INVALID, "hydro_dt must be > 0");
+    if (a->use_drhodt && !(a->previous_dt != 0)) return fail(NNET_ERR_INVALID, "use_drhodt needs previous_dt != 0");
+    NNET_CUDA(cudaSetDevice(h->device));
+    cudaStream_t st = (cudaStream_t)stream;
+
+    KernelInfo ki;
+    if (a->solver == NNET_SOLVER_DENSE_FP64)
+        ki = denseKernel(a->network, a->eos);
+    else if (a->solver == NNET_SOLVER_SPARSE_FP64 || a->solver == NNET_SOLVER_MIXED)
+        ki = sparseKernel(a->network, a->eos, a->solver == NNET_SOLVER_MIXED);
+    else
+        return fail(NNET_ERR_INVALID, "unknown solver");
+    if (!ki.func) return fail(NNET_ERR_INVALID, "solver not available for this network");
+
+    int perSM = 0;
+    NNET_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, ki.func, ki.block, 0));
+    if (perSM < 1) perSM = 1;
+    const size_t maxBlocks = (size_t)h->numSMs * perSM;
+    const size_t need      = (a->num_particles + ki.block - 1) / ki.block;
+    const size_t blocks    = need < maxBlocks ? need : maxBlocks;
+    const size_t slots     = blocks * ki.block;
+    const size_t doubles   = slots * ki.perSlot;
+    if (doubles > h->scratchDoubles)
+    {
+        // grown, never shrunk (as the reference's devData.buffer, parallel_nuclear_net.cu:148)
+        NNET_CUDA(cudaStreamSynchronize(st));
+        if (h->scratch) cudaFree(h->scratch);
+        h->scratch        = nullptr;
+        h->scratchDoubles = 0;
+        NNET_CUDA(cudaMalloc(&h->scratch, doubles * sizeof(double)));
+        h->scratchDoubles = doubles;
+    }
+
+    BurnParams bp{};
+    bp.P = a->num_particles;
+    for (int j = 0; j < a->network; ++j)
+    {
+        if (!a->Y[j]) return fail(NNET_ERR_INVALID, "null species pointer");
+        bp.Y[j] = a->Y[j];
+    }
+    bp.T = a->T, bp.rho = a->rho, bp.rhoM1 = a->rho_m1, bp.dt = a->dt;
+    bp.hydroDt = a->hydro_dt, bp.previousDt = a->previous_dt, bp.mu = a->ideal_gas_mu;
+    bp.useDrhodt = a->use_drhodt && a->rho_m1;
+    bp.maxIter   = a->max_newton_iterations > 0 ? a->max_newton_iterations : 100000;
+    bp.status = a->status, bp.substeps = a->substeps, bp.iterations = a->iterations;
+    bp.queue = h->counters, bp.stats = h->counters + 1, bp.order = nullptr;
+
+    NNET_CUDA(cudaMemsetAsync(h->counters, 0, 8 * sizeof(unsigned long long), st));
+    NetView  nv     = h->nets[ni].view;
+    HelmView hv     = h->helm;
+    double*  sc     = h->scratch;
+    size_t   stride = slots;
+    void*    args[] = {&bp, &nv, &hv, &sc, &stride};
+    NNET_CUDA(cudaLaunchKernel(ki.func, dim3((unsigned)blocks), dim3(ki.block), args, 0, st));
+    h->lastStream = st;
+    return NNET_SUCCESS;
+}
+
+int nnet_get_stats(nnet_handle h, nnet_stats* out)
+{
+    if (!h || !out) return fail(NNET_ERR_INVALID, "null argument");
+    NNET_CUDA(cudaSetDevice(h->device));
+    NNET_CUDA(cudaStreamSynchronize(h->lastStream));
+    unsigned long long v[8];
+    NNET_CUDA(cudaMemcpy(v, h->counters, sizeof v, cudaMemcpyDeviceToHost));
+    out->newton_iterations = v[1];
+    out->substeps          = v[2];
+    for (int s = 0; s < 5; ++s)
+        out->status_count[s] = v[3 + s];
+    return NNET_SUCCESS;
+}
+
+int nnet_helmholtz_eos(nnet_handle h, size_t num_particles, int num_species, const double* Z, const double* T,
+                       const double* rho, double* const* Y, double* u, double* cv, double* p, double* c, double* dpdT,
+                       void* stream)
+{
+    if (!h || !Z || !T || !rho || !Y || !u || !cv || !p || !c || !dpdT) return fail(NNET_ERR_INVALID, "null argument");
+    if (num_species < 1 || num_species > NNET_MAX_SPECIES) return fail(NNET_ERR_INVALID, "bad species count");
+    if (!h->helmLoaded) return fail(NNET_ERR_NO_TABLE, "no Helmholtz table loaded");
+    if (num_particles == 0) return NNET_SUCCESS;
+    NNET_CUDA(cudaSetDevice(h->device));
+    EosParams ep{};
+    ep.P = num_particles, ep.dim = num_species, ep.T = T, ep.rho = rho;
+    for (int j = 0; j < num_species; ++j)
+        ep.Z[j] = Z[j], ep.Y[j] = Y[j];
+    ep.u = u, ep.cv = cv, ep.p = p, ep.c = c, ep.dpdT = dpdT;
+    const int    block  = 128;
+    const size_t blocks = std::min<size_t>((num_particles + block - 1) / block, (size_t)h->numSMs * 16);
+    helmholtzEosKernel<<<(unsigned)blocks, block, 0, (cudaStream_t)stream>>>(ep, h->helm);
+    NNET_CUDA(cudaGetLastError());
+    return NNET_SUCCESS;
+}
+
+} // extern "C"

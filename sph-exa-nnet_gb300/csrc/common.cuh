@@ -1,0 +1,98 @@
+// Shared device definitions of the GB300 burn library: solver constants, per-particle
+// status codes, strided scratch access and the device-side network / table views.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/nnet_gb300.h"
+#include "../data/nnet_network_tables.h"
+
+namespace nnet_gb300
+{
+
+// θ-method Newton substep constants (include/nnet/nuclear_net.hpp:48-106)
+namespace k
+{
+constexpr double theta         = 0.8;
+constexpr double minTemp       = 1e8;
+constexpr double minRho        = 1e5;
+constexpr double maxDtStep     = 2;
+constexpr double minDtStep     = 1e-2;
+constexpr double nanDtStep     = 2e-1;
+constexpr double epsilonSystem = 1e-40;
+constexpr double epsilonVector = 1e-16;
+constexpr double nrMaxDt       = 1e-2;
+constexpr double nrDTTarget    = 1e-2;
+constexpr double nrDTTol       = 4;
+constexpr int    nrMinIt       = 1;
+constexpr int    nrMaxIt       = 11;
+constexpr double nrItTol       = 1e-7;
+constexpr double substepDtTol  = 1e-6;
+} // namespace k
+
+// Element e of scratch slot s lives at base[e * stride + s]: a warp touching element e of
+// 32 consecutive slots reads 256 contiguous bytes.
+template<typename T>
+struct Strided
+{
+    T*     p;
+    size_t s;
+    __device__ __forceinline__ T&      operator[](int e) const { return p[(size_t)e * s]; }
+    __device__ __forceinline__ Strided at(int e) const { return {p + (size_t)e * s, s}; }
+};
+
+// Read-only device view of one network definition (reaction list in CSR form, binding
+// energies, charges, fit / partition-function tables).
+struct NetView
+{
+    int           net, nspec, nreact;
+    const int *   rbeg, *rspec, *rcnt, *pbeg, *pspec, *pcnt;
+    const double *BE, *Z, *z53;
+    const double *fit, *q, *choose;
+    const int *   mainReactant, *secondaryReactant, *mainProduct;
+    const double *eLogT, *eLogRho, *eRate;
+};
+
+// Helmholtz table: one 128-byte line per grid cell (i, j) holding the 13 quantities the
+// EOS outputs depend on, in the order f ft ftt fd fdd fdt fddt fdtt fddtt dpdf dpdft
+// dpdfd dpdfdt (that is, the order the interpolation consumes them), padded to 16.
+constexpr int HELM_IMAX = 541, HELM_JMAX = 201, HELM_CELL = 16;
+struct HelmView
+{
+    const double* cell; // [IMAX][JMAX][16]
+    const double *d, *ddSav, *dd2Sav, *ddiSav, *t, *dtSav, *dt2Sav, *dtiSav, *dt2iSav;
+};
+
+// Per-particle status codes (mirrors nnet_particle_status in the C header)
+enum : int32_t
+{
+    ST_OK       = NNET_PARTICLE_OK,
+    ST_SKIPPED  = NNET_PARTICLE_SKIPPED,
+    ST_LIVELOCK = NNET_PARTICLE_LIVELOCK,
+    ST_MAXITER  = NNET_PARTICLE_MAXITER,
+    ST_ZERO_DT  = NNET_PARTICLE_ZERO_DT,
+};
+
+// Batch arguments as seen by the kernels
+struct BurnParams
+{
+    size_t         P;
+    double*        Y[NNET_MAX_SPECIES];
+    double*        T;
+    const double*  rho;
+    const double*  rhoM1;
+    double*        dt;
+    double         hydroDt, previousDt, mu;
+    int            useDrhodt;
+    long long      maxIter;
+    int32_t*       status;
+    int32_t*       substeps;
+    int32_t*       iterations;
+    unsigned long long* queue;  // work-queue head (reset to 0 before each launch)
+    unsigned long long* stats;  // [0] Newton iterations, [1] substeps, [2+s] status counts
+    const uint32_t*     order;  // optional particle visiting order (nullptr: identity)
+};
+
+} // namespace nnet_gb300

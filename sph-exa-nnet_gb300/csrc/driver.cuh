@@ -1,0 +1,234 @@
+// Persistent burn kernel: one thread per particle, a device work queue, and the θ-method
+// Newton substep state machine of the reference (include/nnet/nuclear_net.hpp:850-959)
+// unrolled into one Newton iteration per loop trip, so that every thread of a warp runs
+// the same iteration code whatever substep or attempt its particle is in.  When a
+// particle finishes (accepted to hydro_dt, fixed point, budget, zero dt) the thread writes
+// it back and pulls the next index from the queue; uneven substep counts therefore never
+// idle a lane while work remains.
+//
+// A solver policy supplies the per-slot scratch views (Y, Yn, DY) and `assembleSolve`,
+// which builds the Newton system around the guess and leaves the solution in DY.
+#pragma once
+
+#include "physics.cuh"
+
+namespace nnet_gb300
+{
+
+template<int NET>
+struct NetDims
+{
+    static constexpr int N = NET;
+    static constexpr int n = NET + 1;
+    static constexpr int R = NET == 14 ? NET14_NUM_REACTIONS : NET == 86 ? NET86_NUM_REACTIONS : NET87_NUM_REACTIONS;
+};
+
+struct ParticleState
+{
+    size_t    p;
+    double    T, dt, elapsed, nextT, attemptDt, rho, drho;
+    long long nit;
+    int       i, nsub;
+};
+
+template<int NET, int EOS>
+__device__ __forceinline__ EosResult evalEos(const NetView& nv, const HelmView& hv, double mu, Strided<double> Yn,
+                                             double T, double rho)
+{
+    if constexpr (EOS == NNET_EOS_IDEAL_GAS) { return idealGasEos(mu, T, rho); }
+    else
+    {
+        // HelmholtzFunctor: abar_ = sum Y, zbar_ = sum Y Z over the network's species
+        // (helmholtz.hpp:217-225; net87 includes the electron entry, Z = -1)
+        double abar = 0, zbar = 0;
+        for (int j = 0; j < NET; ++j)
+            abar = abar + Yn[j];
+        for (int j = 0; j < NET; ++j)
+            zbar += Yn[j] * __ldg(nv.Z + j);
+        return helmholtzEos(hv, abar, zbar, T, rho);
+    }
+}
+
+template<int NET>
+__device__ __forceinline__ void networkRates(const NetView& nv, Strided<double> Yg, double T, double rho,
+                                             Strided<double> BE, Strided<double> rates, Strided<double> drates)
+{
+    if constexpr (NET == 14)
+        net14Rates(nv, T, rho, BE, rates, drates);
+    else if constexpr (NET == 86)
+        net86Rates(nv, T, rho, BE, rates, drates);
+    else
+        net87Rates(nv, Yg[86], T, rho, BE, rates, drates);
+}
+
+// Fetch the next burnable particle; skipped ones (rho <= 1e5 or T <= 1e8,
+// parallel_nuclear_net_impl.cpp:83) are written back immediately.
+template<int NET, class Policy>
+__device__ bool acquire(const BurnParams& bp, Policy& pol, ParticleState& s)
+{
+    for (;;)
+    {
+        unsigned long long q = atomicAdd(bp.queue, 1ull);
+        if (q >= bp.P) return false;
+        const size_t p   = bp.order ? (size_t)bp.order[q] : (size_t)q;
+        const double rho = bp.rho[p], T = bp.T[p];
+        if (!(rho > k::minRho && T > k::minTemp))
+        {
+            if (bp.status) bp.status[p] = ST_SKIPPED;
+            if (bp.substeps) bp.substeps[p] = 0;
+            if (bp.iterations) bp.iterations[p] = 0;
+            atomicAdd(bp.stats + 2 + ST_SKIPPED, 1ull);
+            continue;
+        }
+        for (int j = 0; j < NET; ++j)
+            pol.Y[j] = bp.Y[j][p];
+        double drho = 0;
+        if (bp.useDrhodt && bp.rhoM1 && bp.rhoM1[p] != 0) drho = (rho - bp.rhoM1[p]) / bp.previousDt;
+        s.p = p, s.T = T, s.dt = bp.dt[p], s.elapsed = 0, s.nextT = 0, s.attemptDt = s.dt;
+        s.rho = rho, s.drho = drho, s.nit = 0, s.i = 1, s.nsub = 0;
+        return true;
+    }
+}
+
+template<int NET, class Policy>
+__device__ void release(const BurnParams& bp, Policy& pol, const ParticleState& s, int status)
+{
+    for (int j = 0; j < NET; ++j)
+        bp.Y[j][s.p] = pol.Y[j];
+    bp.T[s.p]  = s.T;
+    bp.dt[s.p] = s.dt;
+    if (bp.status) bp.status[s.p] = status;
+    if (bp.substeps) bp.substeps[s.p] = s.nsub;
+    if (bp.iterations) bp.iterations[s.p] = (int32_t)s.nit;
+    atomicAdd(bp.stats + 0, (unsigned long long)s.nit);
+    atomicAdd(bp.stats + 1, (unsigned long long)s.nsub);
+    atomicAdd(bp.stats + 2 + status, 1ull);
+}
+
+// One Newton iteration of the substep loop.  Returns -1 to continue, or the particle's
+// final status.
+template<int NET, int EOS, class Policy>
+__device__ int newtonIteration(const BurnParams& bp, const NetView& nv, const HelmView& hv, Policy& pol,
+                               ParticleState& s)
+{
+    if (s.i == 1) s.attemptDt = s.dt;
+    if (s.nit >= bp.maxIter) return ST_MAXITER;
+
+    // prepareSystemSubstep (nuclear_net.hpp:858-879)
+    const double dtTot = bp.hydroDt;
+    const double rhoT  = s.rho - s.drho * (dtTot - s.elapsed);
+    double       used  = s.dt;
+    if (dtTot - s.elapsed < s.dt) used = dtTot - s.elapsed;
+    if (used == 0) return ST_ZERO_DT;
+    ++s.nit;
+
+    // prepareSystemNR (nuclear_net.hpp:698-716): θ-blend of the guess
+    double guessT = s.nextT;
+    if (s.i <= 1)
+    {
+        for (int j = 0; j < NET; ++j)
+            pol.Yn[j] = pol.Y[j];
+        guessT = s.T;
+    }
+    const double Ttheta = (1 - k::theta) * s.T + k::theta * guessT;
+    for (int j = 0; j < NET; ++j)
+        pol.Yn[j] = (1 - k::theta) * pol.Y[j] + k::theta * pol.Yn[j];
+    const EosResult eos = evalEos<NET, EOS>(nv, hv, bp.mu, pol.Yn, Ttheta, rhoT);
+
+    pol.assembleSolve(nv, s.T, Ttheta, rhoT, s.drho, eos.cv, eos.dpdT, used);
+
+    // finalizeSystemSubstep (nuclear_net.hpp:891-921) with finalizeSystemNR (:724-782)
+    double usedDt = s.dt;
+    if (dtTot - s.elapsed < s.dt) usedDt = dtTot - s.elapsed;
+    const double lastT = s.nextT;
+    bool         nan   = false;
+    for (int j = 0; j < NET; ++j)
+    {
+        const double v = pol.Y[j] + pol.DY[j + 1];
+        pol.Yn[j]      = v;
+        nan |= isnan(v);
+    }
+    const double T = s.T;
+    s.nextT        = T + pol.DY[0];
+    int  iNext     = s.i;
+    bool conv      = false;
+    double timestep = 0;
+    if (nan || isnan(s.nextT) || s.nextT < 0)
+    {
+        usedDt *= k::nanDtStep;
+        iNext = 0;
+    }
+    else
+    {
+        const double dT_T = fabs((s.nextT - T) / s.nextT);
+        if (s.i >= k::nrMinIt && dT_T > k::nrDTTarget * k::nrDTTol)
+        {
+            usedDt *= k::nrDTTol / dT_T;
+            iNext = 0;
+            for (int j = 0; j < NET; ++j)
+                pol.Yn[j] = pol.Y[j];
+            s.nextT = T;
+        }
+        else
+        {
+            for (int j = 0; j < NET; ++j)
+                if (pol.Yn[j] <= k::epsilonVector) pol.Yn[j] = 0;
+            const double correction = fabs((s.nextT - lastT) / s.nextT);
+            if ((s.i >= k::nrMinIt && correction < k::nrItTol) || s.i >= k::nrMaxIt)
+            {
+                const double dTT = fabs((s.nextT - T) / s.nextT);
+                timestep         = usedDt;
+                usedDt           = (dTT == 0 ? k::maxDtStep : k::nrDTTarget / dTT) * timestep;
+                usedDt           = fmin(usedDt, timestep * k::maxDtStep);
+                usedDt           = fmax(usedDt, timestep * k::minDtStep);
+                usedDt           = fmin(usedDt, k::nrMaxDt);
+                conv             = true;
+            }
+        }
+    }
+    if (dtTot - s.elapsed < s.dt)
+    {
+        if (usedDt < dtTot - s.elapsed) s.dt = usedDt;
+    }
+    else
+        s.dt = usedDt;
+
+    if (conv)
+    {
+        for (int j = 0; j < NET; ++j)
+            pol.Y[j] = pol.Yn[j];
+        s.T = s.nextT;
+        s.elapsed += timestep;
+        ++s.nsub;
+        s.i = 1;
+        if ((dtTot - s.elapsed) / dtTot < k::substepDtTol) return ST_OK;
+        return -1;
+    }
+    if (iNext == 0)
+    {
+        // rejected attempt: with dt unchanged the next attempt replays this one bit for bit
+        if (s.dt == s.attemptDt) return ST_LIVELOCK;
+        s.i = 1;
+        return -1;
+    }
+    s.i = iNext + 1;
+    return -1;
+}
+
+template<int NET, int EOS, class Policy>
+__device__ __forceinline__ void burnLoop(const BurnParams& bp, const NetView& nv, const HelmView& hv, Policy& pol)
+{
+    ParticleState s;
+    bool          have = acquire<NET>(bp, pol, s);
+    while (have)
+    {
+        const int st = newtonIteration<NET, EOS>(bp, nv, hv, pol, s);
+        if (st >= 0)
+        {
+            release<NET>(bp, pol, s, st);
+            have = acquire<NET>(bp, pol, s);
+        }
+    }
+}
+
+} // namespace nnet_gb300

@@ -1,0 +1,256 @@
+"""Python host side of the GB300 burn library, over its C ABI (include/nnet_gb300.h).
+
+Mirrors the reference's plugin surface for the burn path:
+
+  compute_nuclear_reactions(n, first, last, hydro_dt, previous_dt, reactions, rates, eos,
+                            use_drhodt)   <->   nnet::parallel::computeNuclearReactions<true>
+                                               (include/nnet/parallel/parallel_nuclear_net.hpp:86-172)
+  compute_helm_eos(n, first, last, Z)    <->   nnet::parallel::computeHelmEOS<true>
+                                               (parallel_nuclear_net.hpp:191-231)
+
+`n` is any object with the SPH-EXA particle fields the reference requires
+(parallel_nuclear_net.hpp:63-85): `Y` (one 1-D CUDA tensor per species), `temp`, `rho`,
+`rho_m1`, `dt`, and for the EOS `u`, `cv`, `p`, `c`, `dpdT`.  Networks and EOSes are
+passed as the tags below instead of the reference's polymorphic functors.  PyTorch is used
+only for device memory and streams; every computation runs in the library's CUDA kernels,
+and every call fails loudly when the library or a GPU is missing.
+"""
+import ctypes
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libnnet_gb300.so")
+HELM_TABLE_PATH = os.path.join(HERE, "data", "helm_table.bin")
+
+NET14, NET86, NET87 = 14, 86, 87
+EOS_IDEAL_GAS, EOS_HELMHOLTZ = 0, 1
+SOLVER_DENSE_FP64, SOLVER_SPARSE_FP64, SOLVER_MIXED = 0, 1, 2
+STATUS_NAMES = ["OK", "SKIPPED", "LIVELOCK", "MAXITER", "ZERO_DT"]
+NUM_REACTIONS = {14: 29, 86: 309, 87: 311}
+SOLVERS = {"dense": SOLVER_DENSE_FP64, "plain": SOLVER_DENSE_FP64, "sparse": SOLVER_SPARSE_FP64,
+           "mixed": SOLVER_MIXED}
+
+
+class NnetError(RuntimeError):
+    pass
+
+
+class _BurnArgs(ctypes.Structure):
+    _fields_ = [("network", ctypes.c_int), ("eos", ctypes.c_int), ("ideal_gas_mu", ctypes.c_double),
+                ("solver", ctypes.c_int), ("num_particles", ctypes.c_size_t),
+                ("Y", ctypes.POINTER(ctypes.c_void_p)), ("T", ctypes.c_void_p), ("rho", ctypes.c_void_p),
+                ("rho_m1", ctypes.c_void_p), ("dt", ctypes.c_void_p), ("hydro_dt", ctypes.c_double),
+                ("previous_dt", ctypes.c_double), ("use_drhodt", ctypes.c_int),
+                ("max_newton_iterations", ctypes.c_longlong), ("status", ctypes.c_void_p),
+                ("substeps", ctypes.c_void_p), ("iterations", ctypes.c_void_p)]
+
+
+class _Stats(ctypes.Structure):
+    _fields_ = [("newton_iterations", ctypes.c_ulonglong), ("substeps", ctypes.c_ulonglong),
+                ("status_count", ctypes.c_ulonglong * 5)]
+
+
+_lib = None
+
+
+def load_library(path=LIB_PATH):
+    """Load libnnet_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise NnetError(f"{path} is missing: build it with __graft_entry__.build() or sph-exa-nnet_gb300/nnet_build.py")
+    lib = ctypes.CDLL(path)
+    P, I, S, D = ctypes.c_void_p, ctypes.c_int, ctypes.c_size_t, ctypes.c_double
+    lib.nnet_create.argtypes = [I, ctypes.POINTER(P)]
+    lib.nnet_destroy.argtypes = [P]
+    lib.nnet_load_helmholtz_table.argtypes = [P, P]
+    lib.nnet_load_helmholtz_table_file.argtypes = [P, ctypes.c_char_p]
+    lib.nnet_burn.argtypes = [P, ctypes.POINTER(_BurnArgs), P]
+    lib.nnet_get_stats.argtypes = [P, ctypes.POINTER(_Stats)]
+    lib.nnet_helmholtz_eos.argtypes = [P, S, I, P, P, P, P, P, P, P, P, P, P]
+    lib.nnet_network_info.argtypes = [I, ctypes.POINTER(I), ctypes.POINTER(I)]
+    lib.nnet_last_error_message.restype = ctypes.c_char_p
+    _lib = lib
+    return lib
+
+
+def _check(rc):
+    if rc != 0:
+        raise NnetError(f"nnet error {rc}: {_lib.nnet_last_error_message().decode()}")
+
+
+def _ptr(t):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def _require_cuda(t, name):
+    if t is not None and not t.is_cuda:
+        raise NnetError(f"{name} must be a CUDA tensor (the library has no CPU path)")
+
+
+class Context:
+    """One library context (per device): network tables resident in HBM, optional
+    Helmholtz table, and the persistent-kernel scratch."""
+
+    def __init__(self, device=0, helmholtz_table=HELM_TABLE_PATH):
+        import torch
+        if not torch.cuda.is_available():
+            raise NnetError("no CUDA device: the GB300 burn library has no CPU fallback")
+        lib = load_library()
+        self.device = device
+        h = ctypes.c_void_p()
+        _check(lib.nnet_create(device, ctypes.byref(h)))
+        self.handle = h
+        if helmholtz_table is not None:
+            self.load_helmholtz_table(helmholtz_table)
+
+    def close(self):
+        if self.handle:
+            _lib.nnet_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def load_helmholtz_table(self, table):
+        """`table`: path to the binary stand-in, path to a reference-format text table
+        (helm_table.dat), or a float64 array of 21 x 541 x 201 values."""
+        if isinstance(table, str):
+            if table.endswith(".bin"):
+                table = np.fromfile(table, dtype="<f8")
+            else:
+                _check(_lib.nnet_load_helmholtz_table_file(self.handle, table.encode()))
+                return
+        table = np.ascontiguousarray(table, dtype=np.float64).reshape(-1)
+        if table.size != 21 * 541 * 201:
+            raise NnetError("Helmholtz table must hold 21 x 541 x 201 doubles")
+        _check(_lib.nnet_load_helmholtz_table(self.handle, table.ctypes.data_as(ctypes.c_void_p)))
+
+    def burn(self, network, Y, T, rho, dt, hydro_dt, eos=EOS_HELMHOLTZ, mu=0.0, rho_m1=None, previous_dt=0.0,
+             use_drhodt=False, solver=SOLVER_DENSE_FP64, max_iter=100000, status=None, substeps=None,
+             iterations=None, stream=None):
+        """Burn in place.  Y: list of per-species 1-D CUDA float64 tensors (or a 2-D
+        [species, particles] tensor); T, dt updated in place."""
+        import torch
+        if isinstance(solver, str):
+            solver = SOLVERS[solver]
+        if isinstance(eos, str):
+            eos = EOS_IDEAL_GAS if eos.startswith("ideal") else EOS_HELMHOLTZ
+        rows = [Y[j] for j in range(network)]
+        for name, t in [("T", T), ("rho", rho), ("dt", dt), ("rho_m1", rho_m1)] + [("Y", r) for r in rows]:
+            _require_cuda(t, name)
+            if t is not None and t.dtype != torch.float64:
+                raise NnetError(f"{name} must be float64")
+        P = T.numel()
+        yp = (ctypes.c_void_p * network)(*[r.data_ptr() for r in rows])
+        a = _BurnArgs(network=network, eos=eos, ideal_gas_mu=mu, solver=solver, num_particles=P,
+                      Y=ctypes.cast(yp, ctypes.POINTER(ctypes.c_void_p)), T=T.data_ptr(), rho=rho.data_ptr(),
+                      rho_m1=None if rho_m1 is None else rho_m1.data_ptr(), dt=dt.data_ptr(),
+                      hydro_dt=hydro_dt, previous_dt=previous_dt, use_drhodt=int(bool(use_drhodt)),
+                      max_newton_iterations=max_iter,
+                      status=None if status is None else status.data_ptr(),
+                      substeps=None if substeps is None else substeps.data_ptr(),
+                      iterations=None if iterations is None else iterations.data_ptr())
+        s = torch.cuda.current_stream(self.device) if stream is None else stream
+        _check(_lib.nnet_burn(self.handle, ctypes.byref(a), ctypes.c_void_p(s.cuda_stream)))
+
+    def stats(self):
+        st = _Stats()
+        _check(_lib.nnet_get_stats(self.handle, ctypes.byref(st)))
+        return dict(newton_iterations=st.newton_iterations, substeps=st.substeps,
+                    status=dict(zip(STATUS_NAMES, list(st.status_count))))
+
+    def helmholtz_eos(self, Z, T, rho, Y, u, cv, p, c, dpdT, stream=None):
+        import torch
+        Z = np.ascontiguousarray(Z, dtype=np.float64)
+        rows = [Y[j] for j in range(Z.size)]
+        yp = (ctypes.c_void_p * Z.size)(*[r.data_ptr() for r in rows])
+        s = torch.cuda.current_stream(self.device) if stream is None else stream
+        _check(_lib.nnet_helmholtz_eos(self.handle, T.numel(), Z.size, Z.ctypes.data_as(ctypes.c_void_p),
+                                       _ptr(T), _ptr(rho), ctypes.cast(yp, ctypes.c_void_p), _ptr(u), _ptr(cv),
+                                       _ptr(p), _ptr(c), _ptr(dpdT), ctypes.c_void_p(s.cuda_stream)))
+
+
+# ---------------------------------------------------------------- reference-shaped API
+@dataclass(frozen=True)
+class ReactionList:
+    """Tag standing in for nnet::netXX::reactionList."""
+    network: int
+
+
+@dataclass(frozen=True)
+class ComputeReactionRates:
+    """Tag standing in for nnet::netXX::computeReactionRates."""
+    network: int
+
+
+@dataclass(frozen=True)
+class IdealGasFunctor:
+    """nnet::eos::IdealGasFunctor(mu) (ideal_gas.hpp:46-83)."""
+    mu: float
+
+
+@dataclass(frozen=True)
+class HelmholtzFunctor:
+    """nnet::eos::HelmholtzFunctor over the network's charges (helmholtz.hpp:150-226)."""
+    network: int = 86
+
+
+net14_reactionList, net14_computeReactionRates = ReactionList(14), ComputeReactionRates(14)
+net86_reactionList, net86_computeReactionRates = ReactionList(86), ComputeReactionRates(86)
+net87_reactionList, net87_computeReactionRates = ReactionList(87), ComputeReactionRates(87)
+
+_default_context = {}
+
+
+def default_context(device=0):
+    if device not in _default_context:
+        _default_context[device] = Context(device)
+    return _default_context[device]
+
+
+def compute_nuclear_reactions(n, first, last, hydro_dt, previous_dt, reactions, construct_rates_BE, eos,
+                              use_drhodt=False, solver=SOLVER_MIXED, context=None, status=None,
+                              max_iter=100000):
+    """Burn particles [first, last) of `n` over hydro_dt, in place (Y, temp, dt), on the
+    current CUDA stream.  Same parameters as computeNuclearReactions
+    (parallel_nuclear_net.hpp:86-90); `solver` selects the linear-solve form."""
+    if reactions.network != construct_rates_BE.network:
+        raise NnetError("reaction list and rate functor belong to different networks")
+    net = reactions.network
+    if len(n.Y) != net:
+        raise NnetError(f"data holds {len(n.Y)} species, network {net} needs {net}")
+    ctx = context or default_context(n.temp.device.index or 0)
+    sl = slice(first, last)
+    rho_m1 = getattr(n, "rho_m1", None)
+    if use_drhodt and rho_m1 is None:
+        use_drhodt = False  # as the reference when rho_m1 is not allocated (parallel_nuclear_net.hpp:103-114)
+    kw = dict(eos=EOS_IDEAL_GAS, mu=eos.mu) if isinstance(eos, IdealGasFunctor) else dict(eos=EOS_HELMHOLTZ)
+    ctx.burn(net, [y[sl] for y in n.Y], n.temp[sl], n.rho[sl], n.dt[sl], hydro_dt,
+             rho_m1=None if rho_m1 is None else rho_m1[sl], previous_dt=previous_dt, use_drhodt=use_drhodt,
+             solver=solver, status=None if status is None else status[sl], max_iter=max_iter, **kw)
+
+
+def network_charges(network):
+    """Z of a network's species (net87 includes the electron entry, Z = -1)."""
+    import re
+    src = open(os.path.join(HERE, "data", "nnet_network_tables.h")).read()
+    name = "net14_Z" if network == 14 else "net86_Z"
+    body = re.search(name + r"\[\d+\] = \{([^}]*)\}", src).group(1)
+    return np.array([float(v) for v in body.split(",")])[:network]
+
+
+def compute_helm_eos(n, first, last, Z, context=None):
+    """Post-burn Helmholtz EOS into n.u, n.cv, n.p, n.c, n.dpdT for [first, last)
+    (computeHelmEOS, parallel_nuclear_net.hpp:191-261)."""
+    ctx = context or default_context(n.temp.device.index or 0)
+    sl = slice(first, last)
+    ctx.helmholtz_eos(Z, n.temp[sl], n.rho[sl], [y[sl] for y in n.Y], n.u[sl], n.cv[sl], n.p[sl], n.c[sl],
+                      n.dpdT[sl])

@@ -1,0 +1,158 @@
+"""Parity of the CUDA burn path (through the C ABI) with the oracle on the same seeded
+inputs.  Tolerance (from the benchmark spec of the path): relative error <= 1e-8 on every
+Y_i above 1e-12, on T and on the released energy E = sum_i BE_i (Y_i - Y_i0).  Accept/
+reject decisions are discontinuous, so a rounding-level difference can flip a branch for
+an isolated particle; a run passes when at least 99% of particles agree in status and
+values, and every flip is reported."""
+import numpy as np
+import pytest
+
+import workloads
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-8
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import torch
+    import nnet_gb300 as nn
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    c = nn.Context(0)
+    yield c
+    c.close()
+
+
+def gpu_burn(ctx, w, solver, max_iter=20000, **kw):
+    import torch
+    dev = torch.device("cuda:0")
+    Y = torch.tensor(w["Y"], device=dev)
+    T = torch.tensor(w["T"], device=dev)
+    rho = torch.tensor(w["rho"], device=dev)
+    dt = torch.tensor(w["dt"], device=dev)
+    P = T.numel()
+    st = torch.full((P,), -1, dtype=torch.int32, device=dev)
+    it = torch.zeros(P, dtype=torch.int32, device=dev)
+    sub = torch.zeros(P, dtype=torch.int32, device=dev)
+    ctx.burn(w["net"], Y, T, rho, dt, w["hydro_dt"], eos=w["eos"], mu=w["mu"], solver=solver, status=st,
+             iterations=it, substeps=sub, max_iter=max_iter, **kw)
+    torch.cuda.synchronize()
+    return Y.cpu().numpy(), T.cpu().numpy(), dt.cpu().numpy(), st.cpu().numpy(), sub.cpu().numpy(), it.cpu().numpy()
+
+
+def binding_energies(net):
+    import re
+    import os
+    from conftest import PKG
+    src = open(os.path.join(PKG, "data", "nnet_network_tables.h")).read()
+    name = {14: "net14_BE", 86: "net86_BE", 87: "net87_BE"}[net]
+    body = re.search(name + r"\[\d+\] = \{([^}]*)\}", src).group(1)
+    return np.array([float(v) for v in body.split(",")])
+
+
+def compare(w, g, o):
+    """Per-particle agreement mask and worst errors (g: gpu tuple, o: oracle tuple)."""
+    Yg, Tg, dtg, stg = g[:4]
+    Yo, To, dto, sto = o[:4]
+    BE = binding_energies(w["net"])[:, None]
+    Eg = (BE * (Yg - w["Y"])).sum(0)
+    Eo = (BE * (Yo - w["Y"])).sum(0)
+    relT = np.abs(Tg - To) / np.abs(To)
+    big = Yo > 1e-12
+    relY = np.where(big, np.abs(Yg - Yo) / np.where(big, Yo, 1), 0).max(0)
+    relE = np.abs(Eg - Eo) / np.maximum(np.abs(Eo), 1e-300)
+    relE = np.where(np.abs(Eo) > 0, relE, np.abs(Eg - Eo))
+    ok = (stg == sto) & (relT <= TOL) & (relY <= TOL) & ((relE <= TOL) | (np.abs(Eo) < 1e-30 * np.abs(BE).max()))
+    return ok, relT, relY, relE
+
+
+def check(w, g, o, min_frac=0.99):
+    ok, relT, relY, relE = compare(w, g, o)
+    frac = ok.mean()
+    good = ok
+    msg = (f"{w['name']}: agree {ok.sum()}/{ok.size}, status gpu {np.bincount(g[3], minlength=5)} "
+           f"oracle {np.bincount(o[3], minlength=5)}, max rel T {relT[good].max() if good.any() else 0:.2e} "
+           f"Y {relY[good].max() if good.any() else 0:.2e} E {relE[good].max() if good.any() else 0:.2e}")
+    print(msg)
+    assert frac >= min_frac, msg
+    return ok
+
+
+@pytest.mark.parametrize("solver", ["dense"])
+@pytest.mark.parametrize("name,P", [("c1", 4096), ("c2", 512), ("c4", 256)])
+def test_burn_parity(ctx, port, name, P, solver):
+    w = workloads.make(name, P=P, seed=1000 + P)
+    g = gpu_burn(ctx, w, solver)
+    o = port.burn(w["net"], w["Y"], w["T"], w["rho"], w["dt"], w["hydro_dt"], w["eos"], w["mu"], max_iter=20000)
+    check(w, g, o)
+
+
+@pytest.mark.parametrize("solver", ["dense"])
+def test_ideal_gas_net86_and_drhodt(ctx, port, solver):
+    import torch
+    w = workloads.make("c2", P=128, seed=77)
+    w["eos"], w["mu"] = "ideal", 10.0
+    rho_m1 = w["rho"] * 0.998
+    dev = torch.device("cuda:0")
+    Y, T = torch.tensor(w["Y"], device=dev), torch.tensor(w["T"], device=dev)
+    rho, dt = torch.tensor(w["rho"], device=dev), torch.tensor(w["dt"], device=dev)
+    st = torch.zeros(128, dtype=torch.int32, device=dev)
+    ctx.burn(86, Y, T, rho, dt, w["hydro_dt"], eos="ideal", mu=10.0, rho_m1=torch.tensor(rho_m1, device=dev),
+             previous_dt=1e-3, use_drhodt=True, solver=solver, status=st, max_iter=20000)
+    torch.cuda.synchronize()
+    o = port.burn(86, w["Y"], w["T"], w["rho"], w["dt"], w["hydro_dt"], "ideal", 10.0, rho_m1=rho_m1,
+                  previous_dt=1e-3, drhodt_mode=1, max_iter=20000)
+    g = (Y.cpu().numpy(), T.cpu().numpy(), dt.cpu().numpy(), st.cpu().numpy())
+    check(w, g, o)
+
+
+def test_golden_fixture_c2(ctx):
+    """GPU against the reference's own outputs (golden fixture of the c2 sample)."""
+    from conftest import golden
+    gd = golden("burn_c2.npz")
+    w = workloads.make("c2", P=int(gd["P"]))
+    g = gpu_burn(ctx, w, "dense")
+    check(w, g, (gd["Y"], gd["T"], gd["dt"], gd["status"]))
+
+
+def test_edge_cases(ctx):
+    import torch
+    dev = torch.device("cuda:0")
+    w = workloads.make("c1", P=64, seed=9)
+    T = w["T"].copy()
+    rho = w["rho"].copy()
+    T[:4] = 5e7
+    rho[4:8] = 1e4
+    w["T"], w["rho"] = T, rho
+    Y, T2, dt, st, sub, it = gpu_burn(ctx, w, "dense", max_iter=3)
+    assert np.all(st[:8] == 1) and np.array_equal(T2[:8], T[:8]) and np.all(it[:8] == 0)
+    assert np.all(it <= 3) and set(np.unique(st[8:])) <= {0, 2, 3}
+    assert ctx.stats()["status"]["SKIPPED"] == 8
+    # empty batch is a no-op
+    e = torch.zeros(0, dtype=torch.float64, device=dev)
+    ctx.burn(14, [e] * 14, e, e, e, 1e-3, eos="ideal", mu=10.0)
+    # Helmholtz before a table is loaded is an error, not a fault
+    import nnet_gb300 as nn
+    c2 = nn.Context(0, helmholtz_table=None)
+    with pytest.raises(nn.NnetError):
+        c2.burn(86, [e] * 86, e[:0] + torch.ones(1, dtype=torch.float64, device=dev), e, e, 1e-3, eos="helmholtz")
+    c2.close()
+
+
+def test_helmholtz_eos_batch(ctx, port):
+    import torch
+    import nnet_gb300 as nn
+    w = workloads.make("c2", P=1000, seed=5)
+    Z = nn.network_charges(86)
+    dev = torch.device("cuda:0")
+    Y = torch.tensor(w["Y"], device=dev)
+    T, rho = torch.tensor(w["T"], device=dev), torch.tensor(w["rho"], device=dev)
+    outs = [torch.zeros(1000, dtype=torch.float64, device=dev) for _ in range(5)]
+    ctx.helmholtz_eos(Z, T, rho, Y, *outs)
+    torch.cuda.synchronize()
+    ref = port.helm_eos_batch(Z, w["T"], w["rho"], w["Y"])
+    for name, o in zip(["u", "cv", "p", "c", "dpdT"], outs):
+        g = o.cpu().numpy()
+        rel = np.abs(g - ref[name]) / np.abs(ref[name])
+        assert rel.max() < 1e-12, (name, rel.max())

@@ -1,0 +1,94 @@
+"""The oracle restatement against the reference's own outputs (golden fixtures made by
+tests/golden/gen_golden.py from the reference compiled from its sources) and, where that
+build is present, against the reference directly on fresh seeded inputs."""
+import numpy as np
+import pytest
+
+import workloads
+from conftest import golden
+
+RTOL = 1e-12  # bit-exact on the machine that made the fixtures; libm may differ elsewhere
+
+
+def close(a, b, rtol=RTOL):
+    a, b = np.asarray(a), np.asarray(b)
+    both_nan = np.isnan(a) & np.isnan(b)
+    return bool(np.all(both_nan | (np.abs(a - b) <= rtol * np.maximum(np.abs(b), 1e-300))))
+
+
+def test_rate_kat_net14(port):
+    g = golden("rates_kat.npz")
+    BE, r, dr, _ = port.rates(14, g["net14_Y"], 2e9, 1e9, eos="ideal", mu=10.0)
+    assert close(BE, g["net14_BE"]) and close(r, g["net14_rates"]) and close(dr, g["net14_drates"])
+
+
+def test_rate_kat_net87_helmholtz(port):
+    g = golden("rates_kat.npz")
+    BE, r, dr, e = port.rates(87, g["net87_Y"], 3e9, 1e9, eos="helmholtz")
+    assert close(BE, g["net87_BE"]) and close(r, g["net87_rates"]) and close(dr, g["net87_drates"])
+    assert close(e["cv"], g["net87_cv"])
+
+
+def test_rate_points_net86(port):
+    g = golden("rates_kat.npz")
+    for k, (T, rho) in enumerate(g["net86_points"]):
+        BE, r, dr, _ = port.rates(86, g["net86_Y"], T, rho, eos="helmholtz")
+        assert close(r, g["net86_rates"][k]) and close(dr, g["net86_drates"][k]) and close(BE, g["net86_BE"][k])
+
+
+def test_helmholtz_kat(port):
+    g = golden("eos_kat.npz")
+    for k in range(g["T"].size):
+        out = np.array(list(port.helmholtz(g["abar_"][k], g["zbar_"][k], g["T"][k], g["rho"][k]).values()))
+        assert close(out, g["out"][k]), k
+
+
+@pytest.mark.parametrize("name", ["c1", "c2", "c4"])
+def test_burn_golden(port, name):
+    g = golden(f"burn_{name}.npz")
+    w = workloads.make(name, P=int(g["P"]))
+    Y, T, dt, st, sub, it = port.burn(w["net"], w["Y"], w["T"], w["rho"], w["dt"], w["hydro_dt"], w["eos"], w["mu"],
+                                      max_iter=20000)
+    assert np.array_equal(st, g["status"])
+    assert np.array_equal(sub, g["substeps"]) and np.array_equal(it, g["iters"])
+    assert close(T, g["T"]) and close(dt, g["dt"]) and close(Y, g["Y"])
+
+
+def test_solve_nr_trajectory(port):
+    traj = golden("nr_net14.npz")["traj"]
+    Y = workloads.composition(14, 1, 0.5, 0.5, 0.0)[:, 0]
+    T, dt, t = 1e9, 1e-5, 0.0
+    for row in traj:
+        Yn, Tn, dt, ts = port.solve_nr(14, Y, T, 1e9, dt, eos="ideal", mu=10.0)
+        t += ts
+        assert close(np.concatenate([[t, dt, Tn], Yn]), row)
+        Y, T = Yn, Tn
+
+
+def test_port_matches_reference_fresh(port, ref):
+    """Fresh seeds, all three networks, both EOSes, drho/dt on: bit-identical."""
+    for name, P, seed in [("c1", 512, 101), ("c2", 64, 102), ("c4", 48, 103)]:
+        w = workloads.make(name, P=P, seed=seed)
+        for eos in ("ideal", "helmholtz"):
+            rho_m1 = w["rho"] * 0.999
+            a = port.burn(w["net"], w["Y"], w["T"], w["rho"], w["dt"], w["hydro_dt"], eos, 10.0, rho_m1=rho_m1,
+                          previous_dt=1e-3, drhodt_mode=1, max_iter=3000)
+            b = ref.burn(w["net"], w["Y"], w["T"], w["rho"], w["dt"], w["hydro_dt"], eos, 10.0, rho_m1=rho_m1,
+                         previous_dt=1e-3, drhodt_mode=1, max_iter=3000)
+            for x, y in zip(a, b):
+                assert np.array_equal(x, y) or close(x, y, 0.0)
+
+
+def test_skip_and_budget_edge_cases(port):
+    w = workloads.make("c1", P=64, seed=5)
+    T = w["T"].copy()
+    rho = w["rho"].copy()
+    T[:4] = 5e7          # below minTemp: skipped, untouched
+    rho[4:8] = 1e4       # below minRho
+    Y, T2, dt, st, sub, it = port.burn(14, w["Y"], T, rho, w["dt"], 1e-3, "ideal", 10.0, max_iter=2)
+    assert np.all(st[:8] == 1) and np.array_equal(T2[:8], T[:8]) and np.all(it[:8] == 0)
+    assert np.all(it[8:] <= 2)
+    assert set(np.unique(st[8:])) <= {0, 2, 3}
+    # empty batch
+    out = port.burn(14, np.zeros((14, 0)), np.zeros(0), np.zeros(0), np.zeros(0), 1e-3, "ideal", 10.0)
+    assert out[0].shape == (14, 0)

@@ -48,10 +48,10 @@ enum nnet_particle_status
 {
     NNET_PARTICLE_OK       = 0, /* burned to hydro_dt */
     NNET_PARTICLE_SKIPPED  = 1, /* rho <= 1e5 or T <= 1e8: left untouched (parallel_nuclear_net_impl.cpp:83) */
-    NNET_PARTICLE_LIVELOCK = 2, /* the substep loop reached a bit-exact fixed point: a rejected attempt
-                                   left dt unchanged, so the reference would retry it forever
-                                   (nuclear_net.hpp:745-748 with :899-904); state is that of the
-                                   last accepted substep */
+    NNET_PARTICLE_LIVELOCK = 2, /* the substep loop entered a cycle: rejected attempts returned to
+                                   an attempt-start state (dt, Newton temperature) already seen, so
+                                   the reference would retry them forever (nuclear_net.hpp:745-748
+                                   with :899-904); Y and T are those of the last accepted substep */
     NNET_PARTICLE_MAXITER  = 3, /* Newton-iteration budget exhausted */
     NNET_PARTICLE_ZERO_DT  = 4, /* timestep underflowed to 0 (the reference throws, nuclear_net.hpp:533-549) */
 };
@@ -86,6 +86,8 @@ typedef struct
     unsigned long long newton_iterations;
     unsigned long long substeps;
     unsigned long long status_count[5]; /* indexed by nnet_particle_status */
+    unsigned long long refinement_steps; /* NNET_SOLVER_MIXED: FP64-residual refinement steps */
+    unsigned long long fp64_fallbacks;   /* NNET_SOLVER_MIXED: systems re-solved in FP64 */
 } nnet_stats;
 
 /* Arguments of nnet_burn.  All arrays are DEVICE pointers of num_particles entries. */

@@ -9,9 +9,11 @@
 //
 // Additions over the reference (identical in the GPU product):
 //  * a per-particle Newton-iteration budget -> status MAXITER;
-//  * exact detection of the substep-loop fixed point: a rejected attempt that leaves
-//    dt unchanged is replayed bit for bit forever by the reference
-//    (nuclear_net.hpp:745-748 together with :899-904) -> status LIVELOCK;
+//  * exact detection of cycles of the substep loop: between accepted substeps an
+//    attempt is determined by (dt, Newton temperature buffer) alone, and the rejection
+//    rule (nuclear_net.hpp:745-748 together with :899-904) can return to a state it has
+//    seen, after which the reference retries the same attempts forever (period 1 or 2 in
+//    practice); Brent's algorithm on that pair, compared bitwise -> status LIVELOCK;
 //  * dt == 0 at system build (the reference throws, nuclear_net.hpp:533-549) -> ZERO_DT;
 //  * the Newton temperature buffer starts at 0 (uninitialised in the reference,
 //    nuclear_net.hpp:943 and parallel_nuclear_net.cu:65).
@@ -1069,6 +1071,26 @@ void denseSolve(double* M, double* RHS, double* X, int n, double eps)
     }
 }
 
+// Brent cycle detection on the attempt-start state (dt, Newton temperature buffer)
+struct CycleDetector
+{
+    unsigned long long sdt = 0, snt = 0;
+    long               power = 1, steps = 0;
+    static unsigned long long bits(double v)
+    {
+        unsigned long long b;
+        std::memcpy(&b, &v, sizeof b);
+        return b;
+    }
+    void reset(double dt, double nt) { sdt = bits(dt), snt = bits(nt), power = 1, steps = 0; }
+    bool rejected(double dt, double nt)
+    {
+        if (bits(dt) == sdt && bits(nt) == snt) return true;
+        if (++steps == power) sdt = bits(dt), snt = bits(nt), power <<= 1, steps = 0;
+        return false;
+    }
+};
+
 struct Work
 {
     std::vector<double> Mp, RHS, DY, Ybuf, Y, rates;
@@ -1133,12 +1155,13 @@ int burnOne(const Ctx& c, Work& w, double* Y, double& T, double rho, double drho
             long max_iter, int& nsub, long& nit)
 {
     const int dim = c.dim;
-    double    nextT = 0, elapsed = 0, attempt_dt = dt;
-    double*   nextY = w.Ybuf.data();
+    double        nextT = 0, elapsed = 0;
+    double*       nextY = w.Ybuf.data();
+    CycleDetector cd;
+    cd.reset(dt, nextT);
     nsub = 0, nit = 0;
     for (int i = 1;; ++i)
     {
-        if (i == 1) attempt_dt = dt;
         if (nit >= max_iter) return ST_MAXITER;
         // prepareSystemSubstep
         const double rho_t = rho - drho_dt * (dt_tot - elapsed);
@@ -1180,8 +1203,9 @@ int burnOne(const Ctx& c, Work& w, double* Y, double& T, double rho, double drho
             elapsed += timestep;
             ++nsub;
             if ((dt_tot - elapsed) / dt_tot < kSubstepDtTol) return ST_OK;
+            cd.reset(dt, nextT);
         }
-        else if (i == 0 && dt == attempt_dt)
+        else if (i == 0 && cd.rejected(dt, nextT))
             return ST_LIVELOCK;
     }
 }

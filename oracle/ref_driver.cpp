@@ -39,6 +39,29 @@ extern double f[IMAX][JMAX], fd[IMAX][JMAX], ft[IMAX][JMAX], fdd[IMAX][JMAX], ft
 
 namespace
 {
+// Exact cycle detection on the state an attempt starts from.  Between accepted substeps
+// Y, T and the elapsed time do not change, so an attempt is fully determined by
+// (dt, Newton temperature buffer); once that pair repeats, the reference's substep loop
+// replays the same rejected attempts forever.  Brent's algorithm, compared bitwise.
+struct CycleDetector
+{
+    unsigned long long sdt = 0, snt = 0;
+    long               power = 1, steps = 0;
+    static unsigned long long bits(double v)
+    {
+        unsigned long long b;
+        std::memcpy(&b, &v, sizeof b);
+        return b;
+    }
+    void reset(double dt, double nt) { sdt = bits(dt), snt = bits(nt), power = 1, steps = 0; }
+    bool rejected(double dt, double nt)
+    {
+        if (bits(dt) == sdt && bits(nt) == snt) return true;
+        if (++steps == power) sdt = bits(dt), snt = bits(nt), power <<= 1, steps = 0;
+        return false;
+    }
+};
+
 enum Status
 {
     ST_OK       = 0,
@@ -165,10 +188,11 @@ int ref_burn(int net, int eos_kind, double mu, size_t P, double* Y, double* T, c
                 double drho_dt = 0;
                 if (drhodt_mode == 1 && rho_m1 && rho_m1[p] != 0) drho_dt = (rho[p] - rho_m1[p]) / previous_dt;
 
-                double final_T = T[p], next_T = 0, elapsed = 0, pdt = dt[p], attempt_dt = pdt;
+                double        final_T = T[p], next_T = 0, elapsed = 0, pdt = dt[p];
+                CycleDetector cd;
+                cd.reset(pdt, next_T);
                 for (int i = 1;; ++i)
                 {
-                    if (i == 1) attempt_dt = pdt;
                     if (nit >= max_iter)
                     {
                         st = ST_MAXITER;
@@ -196,10 +220,13 @@ int ref_burn(int net, int eos_kind, double mu, size_t P, double* Y, double* T, c
                     if (i == 0)
                     {
                         if (elapsed != elapsed0)
-                            ++nsub; // accepted substep
-                        else if (pdt == attempt_dt)
                         {
-                            st = ST_LIVELOCK; // rejected attempt with unchanged dt replays forever
+                            ++nsub; // accepted substep
+                            cd.reset(pdt, next_T);
+                        }
+                        else if (cd.rejected(pdt, next_T))
+                        {
+                            st = ST_LIVELOCK; // the rejected attempts cycle: the reference loops forever
                             break;
                         }
                     }

@@ -11,6 +11,7 @@
 
 #include "physics.cuh"
 #include "launch.hpp"
+#include "sparse_plan.hpp"
 
 using namespace nnet_gb300;
 
@@ -35,8 +36,9 @@ int fail(int code, const std::string& msg)
 // one device allocation per network holding every table of NetView
 struct NetBuffer
 {
-    void*   mem = nullptr;
-    NetView view{};
+    void*      mem = nullptr;
+    NetView    view{};
+    SparsePlan plan;
 };
 
 int uploadNetwork(int net, NetBuffer& b)
@@ -95,6 +97,17 @@ int uploadNetwork(int net, NetBuffer& b)
     const size_t oPb = puti(pbeg, R + 1), oPs = puti(pspec, np), oPc = puti(pcnt, np);
     const size_t oMr = puti(net86_main_reactant, 157), oSr = puti(net86_secondary_reactant, 157),
                  oMp = puti(net86_main_product, 157);
+    // sparse-solver plan (symbolic analysis of this network's Newton matrix)
+    const SparsePlan sp = buildSparsePlan(net, rbeg, rspec, rcnt, pbeg, pspec, pcnt, R);
+    b.plan              = sp;
+    const size_t oCoef  = putd(sp.cCoef.data(), sp.cCoef.size());
+    auto         putv   = [&](const std::vector<int>& v) { return puti(v.data(), v.size()); };
+    const size_t oPerm = putv(sp.perm), oIperm = putv(sp.iperm), oRowBeg = putv(sp.rowBeg), oPosRow = putv(sp.posRow),
+                 oPosCol = putv(sp.posCol), oKPiv = putv(sp.kPiv), oLBeg = putv(sp.lBeg), oLPos = putv(sp.lPos),
+                 oLRow = putv(sp.lRow), oTBeg = putv(sp.tBeg), oUBeg = putv(sp.uBeg), oUPos = putv(sp.uPos),
+                 oUCol = putv(sp.uCol), oTPos = putv(sp.tPos), oDiag = putv(sp.diagPos), oCol0 = putv(sp.col0Pos),
+                 oRow0 = putv(sp.row0Pos), oCBeg = putv(sp.cBeg), oCPos = putv(sp.cPos), oCRow = putv(sp.cRow),
+                 oSb = putv(sp.sbPos), oSbD = putv(sp.sbDiag);
     const size_t bytesD = d.size() * sizeof(double), bytes = bytesD + ii.size() * sizeof(int);
     NNET_CUDA(cudaMalloc(&b.mem, bytes));
     NNET_CUDA(cudaMemcpy(b.mem, d.data(), bytesD, cudaMemcpyHostToDevice));
@@ -107,8 +120,17 @@ int uploadNetwork(int net, NetBuffer& b)
     v.BE = D + oBE, v.Z = D + oZ, v.z53 = D + oZ53, v.fit = D + oFit, v.q = D + oQ, v.choose = D + oCh;
     v.mainReactant = I + oMr, v.secondaryReactant = I + oSr, v.mainProduct = I + oMp;
     v.eLogT = D + oLT, v.eLogRho = D + oLR, v.eRate = D + oER;
+    SparseView& w = v.sp;
+    w.n = sp.n, w.nnz = sp.nnz, w.nsb = (int)sp.sbPos.size(), w.pos00 = sp.pos00, w.tNew = sp.iperm[0];
+    w.perm = I + oPerm, w.iperm = I + oIperm, w.rowBeg = I + oRowBeg, w.posRow = I + oPosRow, w.posCol = I + oPosCol;
+    w.kPiv = I + oKPiv, w.lBeg = I + oLBeg, w.lPos = I + oLPos, w.lRow = I + oLRow, w.tBeg = I + oTBeg;
+    w.uBeg = I + oUBeg, w.uPos = I + oUPos, w.uCol = I + oUCol, w.tPos = I + oTPos;
+    w.diagPos = I + oDiag, w.col0Pos = I + oCol0, w.row0Pos = I + oRow0, w.cBeg = I + oCBeg, w.cPos = I + oCPos;
+    w.cRow = I + oCRow, w.sbPos = I + oSb, w.sbDiag = I + oSbD, w.cCoef = D + oCoef;
     return NNET_SUCCESS;
 }
+
+constexpr int kCounters = 16;
 
 int netIndex(int net) { return net == 14 ? 0 : net == 86 ? 1 : net == 87 ? 2 : -1; }
 
@@ -149,7 +171,7 @@ struct nnet_context
     bool                helmLoaded = false;
     double*             scratch    = nullptr;
     size_t              scratchDoubles = 0;
-    unsigned long long* counters   = nullptr; // [0] queue, [1..7] stats
+    unsigned long long* counters   = nullptr; // [0] queue, [1..] stats (see BurnParams::stats)
     cudaStream_t        lastStream = nullptr;
 };
 
@@ -183,12 +205,12 @@ int nnet_create(int device, nnet_handle* out)
             return rc;
         }
     }
-    if (cudaMalloc(&h->counters, 8 * sizeof(unsigned long long)) != cudaSuccess)
+    if (cudaMalloc(&h->counters, kCounters * sizeof(unsigned long long)) != cudaSuccess)
     {
         nnet_destroy(h);
         return fail(NNET_ERR_CUDA, "cudaMalloc counters");
     }
-    cudaMemset(h->counters, 0, 8 * sizeof(unsigned long long));
+    cudaMemset(h->counters, 0, kCounters * sizeof(unsigned long long));
     *out = h;
     return NNET_SUCCESS;
 }
@@ -314,6 +336,8 @@ int nnet_burn(nnet_handle h, const nnet_burn_args* a, void* stream)
     else
         return fail(NNET_ERR_INVALID, "unknown solver");
     if (!ki.func) return fail(NNET_ERR_INVALID, "solver not available for this network");
+    if (ki.maxNnz && h->nets[ni].plan.nnz > ki.maxNnz)
+        return fail(NNET_ERR_TOO_LARGE, "sparse factor does not fit the kernel's storage");
 
     int perSM = 0;
     NNET_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, ki.func, ki.block, 0));
@@ -348,7 +372,7 @@ int nnet_burn(nnet_handle h, const nnet_burn_args* a, void* stream)
     bp.status = a->status, bp.substeps = a->substeps, bp.iterations = a->iterations;
     bp.queue = h->counters, bp.stats = h->counters + 1, bp.order = nullptr;
 
-    NNET_CUDA(cudaMemsetAsync(h->counters, 0, 8 * sizeof(unsigned long long), st));
+    NNET_CUDA(cudaMemsetAsync(h->counters, 0, kCounters * sizeof(unsigned long long), st));
     NetView  nv     = h->nets[ni].view;
     HelmView hv     = h->helm;
     double*  sc     = h->scratch;
@@ -364,12 +388,14 @@ int nnet_get_stats(nnet_handle h, nnet_stats* out)
     if (!h || !out) return fail(NNET_ERR_INVALID, "null argument");
     NNET_CUDA(cudaSetDevice(h->device));
     NNET_CUDA(cudaStreamSynchronize(h->lastStream));
-    unsigned long long v[8];
+    unsigned long long v[kCounters];
     NNET_CUDA(cudaMemcpy(v, h->counters, sizeof v, cudaMemcpyDeviceToHost));
     out->newton_iterations = v[1];
     out->substeps          = v[2];
     for (int s = 0; s < 5; ++s)
         out->status_count[s] = v[3 + s];
+    out->refinement_steps = v[8];
+    out->fp64_fallbacks   = v[9];
     return NNET_SUCCESS;
 }
 

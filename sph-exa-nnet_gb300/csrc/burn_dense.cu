@@ -179,6 +179,8 @@ struct DensePolicy
             DY[i] = res;
         }
     }
+
+    __device__ __forceinline__ double dy(const SparseView&, int i) const { return DY[i]; }
 };
 
 template<int NET, int EOS>
@@ -193,7 +195,7 @@ __global__ void __launch_bounds__(128) burnDenseKernel(BurnParams bp, NetView nv
 template<int NET, int EOS>
 static KernelInfo denseInfo()
 {
-    return {(const void*)burnDenseKernel<NET, EOS>, DensePolicy<NET>::perSlot(), 128};
+    return {(const void*)burnDenseKernel<NET, EOS>, DensePolicy<NET>::perSlot(), 128, 0};
 }
 
 KernelInfo denseKernel(int net, int eos)

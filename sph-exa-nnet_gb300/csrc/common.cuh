@@ -43,6 +43,16 @@ struct Strided
     __device__ __forceinline__ Strided at(int e) const { return {p + (size_t)e * s, s}; }
 };
 
+// Device view of a network's sparse-solver plan (see sparse_plan.hpp for the meaning)
+struct SparseView
+{
+    int           n, nnz, nsb, pos00, tNew; // tNew: position of the temperature in the new order
+    const int *   perm, *iperm, *rowBeg, *posRow, *posCol, *kPiv, *lBeg, *lPos, *lRow, *tBeg, *uBeg, *uPos, *uCol,
+        *tPos;
+    const int *   diagPos, *col0Pos, *row0Pos, *cBeg, *cPos, *cRow, *sbPos, *sbDiag;
+    const double* cCoef;
+};
+
 // Read-only device view of one network definition (reaction list in CSR form, binding
 // energies, charges, fit / partition-function tables).
 struct NetView
@@ -53,6 +63,7 @@ struct NetView
     const double *fit, *q, *choose;
     const int *   mainReactant, *secondaryReactant, *mainProduct;
     const double *eLogT, *eLogRho, *eRate;
+    SparseView    sp;
 };
 
 // Helmholtz table: one 128-byte line per grid cell (i, j) holding the 13 quantities the
@@ -91,7 +102,8 @@ struct BurnParams
     int32_t*       substeps;
     int32_t*       iterations;
     unsigned long long* queue;  // work-queue head (reset to 0 before each launch)
-    unsigned long long* stats;  // [0] Newton iterations, [1] substeps, [2+s] status counts
+    unsigned long long* stats;  // [0] Newton iterations, [1] substeps, [2+s] status counts,
+                                // [7] refinement steps, [8] FP64 fallbacks
     const uint32_t*     order;  // optional particle visiting order (nullptr: identity)
 };
 

@@ -25,10 +25,28 @@ struct NetDims
 
 struct ParticleState
 {
-    size_t    p;
-    double    T, dt, elapsed, nextT, attemptDt, rho, drho;
-    long long nit;
-    int       i, nsub;
+    size_t             p;
+    double             T, dt, elapsed, nextT, rho, drho;
+    long long          nit;
+    int                i, nsub;
+    unsigned long long cdDt, cdNt; // cycle detection: saved attempt-start state (bits)
+    int                cdPower, cdSteps;
+
+    // Between accepted substeps an attempt is fully determined by (dt, Newton temperature
+    // buffer); Brent's algorithm on that pair, compared bitwise, detects the cycles in
+    // which the reference's rejection rule (nuclear_net.hpp:745-748 with :899-904)
+    // retries the same attempts forever.
+    __device__ __forceinline__ void cycleReset()
+    {
+        cdDt = __double_as_longlong(dt), cdNt = __double_as_longlong(nextT), cdPower = 1, cdSteps = 0;
+    }
+    __device__ __forceinline__ bool cycleRejected()
+    {
+        const unsigned long long a = __double_as_longlong(dt), b = __double_as_longlong(nextT);
+        if (a == cdDt && b == cdNt) return true;
+        if (++cdSteps == cdPower) cdDt = a, cdNt = b, cdPower <<= 1, cdSteps = 0;
+        return false;
+    }
 };
 
 template<int NET, int EOS>
@@ -84,8 +102,9 @@ __device__ bool acquire(const BurnParams& bp, Policy& pol, ParticleState& s)
             pol.Y[j] = bp.Y[j][p];
         double drho = 0;
         if (bp.useDrhodt && bp.rhoM1 && bp.rhoM1[p] != 0) drho = (rho - bp.rhoM1[p]) / bp.previousDt;
-        s.p = p, s.T = T, s.dt = bp.dt[p], s.elapsed = 0, s.nextT = 0, s.attemptDt = s.dt;
+        s.p = p, s.T = T, s.dt = bp.dt[p], s.elapsed = 0, s.nextT = 0;
         s.rho = rho, s.drho = drho, s.nit = 0, s.i = 1, s.nsub = 0;
+        s.cycleReset();
         return true;
     }
 }
@@ -111,7 +130,6 @@ template<int NET, int EOS, class Policy>
 __device__ int newtonIteration(const BurnParams& bp, const NetView& nv, const HelmView& hv, Policy& pol,
                                ParticleState& s)
 {
-    if (s.i == 1) s.attemptDt = s.dt;
     if (s.nit >= bp.maxIter) return ST_MAXITER;
 
     // prepareSystemSubstep (nuclear_net.hpp:858-879)
@@ -144,12 +162,12 @@ __device__ int newtonIteration(const BurnParams& bp, const NetView& nv, const He
     bool         nan   = false;
     for (int j = 0; j < NET; ++j)
     {
-        const double v = pol.Y[j] + pol.DY[j + 1];
+        const double v = pol.Y[j] + pol.dy(nv.sp, j + 1);
         pol.Yn[j]      = v;
         nan |= isnan(v);
     }
     const double T = s.T;
-    s.nextT        = T + pol.DY[0];
+    s.nextT        = T + pol.dy(nv.sp, 0);
     int  iNext     = s.i;
     bool conv      = false;
     double timestep = 0;
@@ -202,12 +220,13 @@ __device__ int newtonIteration(const BurnParams& bp, const NetView& nv, const He
         ++s.nsub;
         s.i = 1;
         if ((dtTot - s.elapsed) / dtTot < k::substepDtTol) return ST_OK;
+        s.cycleReset();
         return -1;
     }
     if (iNext == 0)
     {
-        // rejected attempt: with dt unchanged the next attempt replays this one bit for bit
-        if (s.dt == s.attemptDt) return ST_LIVELOCK;
+        // rejected attempt: a repeated attempt-start state means the loop never ends
+        if (s.cycleRejected()) return ST_LIVELOCK;
         s.i = 1;
         return -1;
     }

@@ -49,7 +49,7 @@ def build(force=False, verbose=False):
     nvcc = _nvcc()
     headers = glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.hpp")) + [
         os.path.join(HERE, "..", "include", "nnet_gb300.h"), os.path.join(HERE, "data", "nnet_network_tables.h")]
-    srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
     objs = []
     jobs = []
     for s in srcs:
@@ -57,8 +57,6 @@ def build(force=False, verbose=False):
         objs.append(o)
         if force or _stale(o, [s] + headers):
             cmd = [nvcc, *ARCH, *NVCC_FLAGS, "-c", s, "-o", o]
-            if os.path.basename(s).startswith("burn_dense"):
-                pass
             jobs.append(cmd)
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         for cmd, r in zip(jobs, ex.map(lambda c: subprocess.run(c, capture_output=True, text=True), jobs)):

@@ -50,7 +50,8 @@ class _BurnArgs(ctypes.Structure):
 
 class _Stats(ctypes.Structure):
     _fields_ = [("newton_iterations", ctypes.c_ulonglong), ("substeps", ctypes.c_ulonglong),
-                ("status_count", ctypes.c_ulonglong * 5)]
+                ("status_count", ctypes.c_ulonglong * 5), ("refinement_steps", ctypes.c_ulonglong),
+                ("fp64_fallbacks", ctypes.c_ulonglong)]
 
 
 _lib = None
@@ -165,7 +166,8 @@ class Context:
         st = _Stats()
         _check(_lib.nnet_get_stats(self.handle, ctypes.byref(st)))
         return dict(newton_iterations=st.newton_iterations, substeps=st.substeps,
-                    status=dict(zip(STATUS_NAMES, list(st.status_count))))
+                    status=dict(zip(STATUS_NAMES, list(st.status_count))), refinement_steps=st.refinement_steps,
+                    fp64_fallbacks=st.fp64_fallbacks)
 
     def helmholtz_eos(self, Z, T, rho, Y, u, cv, p, c, dpdT, stream=None):
         import torch

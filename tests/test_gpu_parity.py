@@ -79,7 +79,7 @@ def check(w, g, o, min_frac=0.99):
     return ok
 
 
-@pytest.mark.parametrize("solver", ["dense"])
+@pytest.mark.parametrize("solver", ["dense", "sparse", "mixed"])
 @pytest.mark.parametrize("name,P", [("c1", 4096), ("c2", 512), ("c4", 256)])
 def test_burn_parity(ctx, port, name, P, solver):
     w = workloads.make(name, P=P, seed=1000 + P)
@@ -88,7 +88,7 @@ def test_burn_parity(ctx, port, name, P, solver):
     check(w, g, o)
 
 
-@pytest.mark.parametrize("solver", ["dense"])
+@pytest.mark.parametrize("solver", ["dense", "sparse", "mixed"])
 def test_ideal_gas_net86_and_drhodt(ctx, port, solver):
     import torch
     w = workloads.make("c2", P=128, seed=77)
@@ -107,12 +107,13 @@ def test_ideal_gas_net86_and_drhodt(ctx, port, solver):
     check(w, g, o)
 
 
-def test_golden_fixture_c2(ctx):
+@pytest.mark.parametrize("solver", ["dense", "mixed"])
+def test_golden_fixture_c2(ctx, solver):
     """GPU against the reference's own outputs (golden fixture of the c2 sample)."""
     from conftest import golden
     gd = golden("burn_c2.npz")
     w = workloads.make("c2", P=int(gd["P"]))
-    g = gpu_burn(ctx, w, "dense")
+    g = gpu_burn(ctx, w, solver)
     check(w, g, (gd["Y"], gd["T"], gd["dt"], gd["status"]))
 
 

@@ -262,9 +262,13 @@ def main():
 
     # ---- roofline: FP64 pipe (the kernel computes in FP64; no HBM or tensor bound applies)
     iters = stats["newton_iterations"]
-    flops_per_iter = FLOPS_PER_ITER[solver]
-    achieved = flops_per_iter * iters / (kernel_ms / 1e3) / 1e12
-    peak = FP64_PEAK_TFLOPS
+    flops_per_iter = algorithmic_flops(nn, 86, solver)
+    refine_flops = 2 * nn.solver_info(86, "sparse")[2] * stats["refinement_steps"]
+    achieved = (flops_per_iter * iters + refine_flops) / (kernel_ms / 1e3) / 1e12
+    try:
+        peak, peak_src = nn.measure_fp64_peak(local), "FP64 FMA probe kernel measured live in this run"
+    except Exception:
+        peak, peak_src = FP64_PEAK_TFLOPS, "nominal GB300 FP64 (probe failed)"
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, workload c2 distributions)",
@@ -276,8 +280,9 @@ def main():
             "gpu_launches": args.steps,
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak, "traffic": None,
-                         "peak_source": "nominal GB300 FP64 (no FP64 figure in MEASURED_PEAKS.json)",
-                         "flops_per_newton_iteration": flops_per_iter},
+                         "peak_source": peak_src + "; MEASURED_PEAKS.json has no FP64 figure",
+                         "flops_per_newton_iteration": flops_per_iter,
+                         "refinement_steps": stats["refinement_steps"], "fp64_fallbacks": stats["fp64_fallbacks"]},
             "kernel_ms": kernel_ms, "wall_s": wall, "clocks": clk.summary()}
     if plain:
         line["plain_fp64"] = plain
@@ -294,11 +299,21 @@ def main():
         dist.destroy_process_group()
 
 
-# algorithmic FP64 FLOPs per Newton iteration of net86: dense Gaussian
-# elimination of the 87 x 87 system as the reference performs it (n^3/3 multiply-adds,
-# full fill) plus the system assembly; the sparse forms count only the operations of the
-# fill-reducing factorisation they execute.
-FLOPS_PER_ITER = {"dense": 2 * 223_213 + 2 * 87 * 87 + 2 * (309 * 6 + 2 * 87 * 87), "sparse": 0, "mixed": 0}
+def algorithmic_flops(nn, net, solver):
+    """Algorithmic FP64 FLOPs of one Newton iteration: the linear solve as the form executes it
+    (2 x multiply-adds of factorisation and triangular solves, plus the divisions), and the
+    system assembly 2 (R (k^2 + k) + entries) with k = 2 reactants per reaction.  The mixed
+    form's FP32 factorisation is not FP64 work; its FP64 residuals are added per refinement
+    step from the run's counters.  Rate and EOS transcendentals are not counted as FLOPs."""
+    n = net + 1
+    R = nn.NUM_REACTIONS[net]
+    f, s, e = nn.solver_info(net, "dense" if solver == "dense" else "sparse")
+    if solver == "dense":
+        return 2 * (f + s) + n * (n + 1) // 2 + 2 * (R * 6 + n * n)
+    lu = 0 if solver == "mixed" else 2 * (f + s) + n
+    return lu + 2 * (R * 6 + e)
+
+
 FP64_PEAK_TFLOPS = 1.25
 
 if __name__ == "__main__":

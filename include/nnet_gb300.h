@@ -143,6 +143,66 @@ int nnet_helmholtz_eos(nnet_handle h, size_t num_particles, int num_species, con
                        const double* T, const double* rho, double* const* Y, double* u, double* cv,
                        double* p, double* c, double* dpdT, void* stream);
 
+/* ---------------------------------------------------------------- burn server
+ * Continuous batching of burn requests on one GPU (no reference counterpart: the
+ * reference burns one caller-provided batch per blocking call).  Requests are admitted
+ * FIFO while their device footprint fits `hbm_budget_bytes` and a workspace is free; the
+ * state of an admitted request stays on the device until it completes; admitted requests
+ * run concurrently as time slices of `slice_iterations` Newton iterations per particle,
+ * so requests arriving while others run start as soon as memory frees up.  Slicing does
+ * not change any particle's arithmetic: results equal an unsliced nnet_burn bit for bit. */
+typedef struct nnet_server_s* nnet_server;
+
+typedef struct
+{
+    double    hbm_budget_bytes;        /* device bytes of admitted request state; <= 0: 150e9 */
+    int       solver;                  /* nnet_solver */
+    long long slice_iterations;        /* Newton iterations per particle per slice; <= 0: 64 */
+    int       max_concurrent_requests; /* resident requests (1..64), one workspace each */
+} nnet_server_config;
+
+typedef struct
+{
+    int           network, eos;
+    double        ideal_gas_mu;
+    size_t        num_particles;
+    double*       Y;      /* HOST, species-major [network][num_particles]; overwritten with results */
+    double*       T;      /* HOST, in/out */
+    const double* rho;    /* HOST */
+    double*       dt;     /* HOST, in/out */
+    int32_t*      status; /* HOST, optional: nnet_particle_status per particle */
+    double        hydro_dt;
+    long long     max_newton_iterations; /* <= 0 selects 100000 */
+} nnet_request;
+
+typedef struct
+{
+    unsigned long long completed_requests;
+    double             completed_particles;
+    double             span_seconds;  /* first submission to last completion */
+    double             latency_p50, latency_p95, latency_p99, latency_max; /* seconds */
+    unsigned long long slices;        /* kernel launches issued */
+} nnet_server_stats;
+
+int nnet_server_create(nnet_handle h, const nnet_server_config* cfg, nnet_server* out);
+/* Queue a request (host buffers must stay valid until nnet_server_wait returns). */
+int nnet_server_submit(nnet_server s, const nnet_request* r, uint64_t* id);
+/* done = 1 when the results are in the host buffers, -1 on failure, 0 otherwise. */
+int nnet_server_query(nnet_server s, uint64_t id, int* done);
+/* Block until request `id` completed; latency = completion - submission (seconds). */
+int nnet_server_wait(nnet_server s, uint64_t id, double* latency_seconds);
+int nnet_server_get_stats(nnet_server s, nnet_server_stats* out);
+/* Finish every queued request, then release the server. */
+int nnet_server_destroy(nnet_server s);
+
+/* Operation counts of one Newton-iteration linear solve of `network` with `solver`
+ * (no reference counterpart; used for roofline accounting): multiply-adds of the
+ * factorisation and of one pair of triangular solves, and the stored factor entries. */
+int nnet_solver_info(int network, int solver, long long* factor_fma, long long* solve_fma, int* factor_entries);
+/* Measured FP64 fused-multiply-add throughput of `device` in TFLOP/s (2 flops per FMA)
+ * with a dependency-free probe kernel (no reference counterpart; roofline denominator). */
+int nnet_measure_fp64_peak(int device, double* tflops);
+
 /* Number of species / reactions of a network, 0 on success. */
 int nnet_network_info(int network, int* num_species, int* num_reactions);
 /* Human-readable description of the last error on this thread. */

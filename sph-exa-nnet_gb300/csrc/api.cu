@@ -1,5 +1,6 @@
 // C ABI of the GB300 burn library (include/nnet_gb300.h): context, table upload, burn
 // dispatch and the post-burn Helmholtz EOS.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -12,6 +13,7 @@
 #include "physics.cuh"
 #include "launch.hpp"
 #include "sparse_plan.hpp"
+#include "context.hpp"
 
 using namespace nnet_gb300;
 
@@ -32,14 +34,6 @@ int fail(int code, const std::string& msg)
         if (e_ != cudaSuccess)                                                                                        \
             return fail(NNET_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));                           \
     } while (0)
-
-// one device allocation per network holding every table of NetView
-struct NetBuffer
-{
-    void*      mem = nullptr;
-    NetView    view{};
-    SparsePlan plan;
-};
 
 int uploadNetwork(int net, NetBuffer& b)
 {
@@ -162,19 +156,6 @@ __global__ void helmholtzEosKernel(EosParams ep, HelmView hv)
 }
 } // namespace
 
-struct nnet_context
-{
-    int                 device = 0, numSMs = 0;
-    NetBuffer           nets[3];
-    void*               helmMem    = nullptr;
-    HelmView            helm{};
-    bool                helmLoaded = false;
-    double*             scratch    = nullptr;
-    size_t              scratchDoubles = 0;
-    unsigned long long* counters   = nullptr; // [0] queue, [1..] stats (see BurnParams::stats)
-    cudaStream_t        lastStream = nullptr;
-};
-
 extern "C" {
 
 const char* nnet_last_error_message(void) { return g_lastError.c_str(); }
@@ -185,6 +166,41 @@ int nnet_network_info(int network, int* num_species, int* num_reactions)
     if (num_species) *num_species = network;
     if (num_reactions)
         *num_reactions = network == 14 ? NET14_NUM_REACTIONS : network == 86 ? NET86_NUM_REACTIONS : NET87_NUM_REACTIONS;
+    return NNET_SUCCESS;
+}
+
+int nnet_solver_info(int network, int solver, long long* factor_fma, long long* solve_fma, int* factor_entries)
+{
+    const int R = network == 14 ? NET14_NUM_REACTIONS : network == 86 ? NET86_NUM_REACTIONS : NET87_NUM_REACTIONS;
+    if (netIndex(network) < 0) return fail(NNET_ERR_INVALID, "unknown network");
+    const int n = network + 1;
+    if (solver == NNET_SOLVER_DENSE_FP64)
+    {
+        // eigen::solve with complete fill (eigen.hpp:155-198): elimination of row i by rows
+        // j < i costs 1 + (n - 1 - j) multiply-adds, back substitution n(n-1)/2
+        long long f = 0;
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < i; ++j)
+                f += 1 + (n - 1 - j);
+        if (factor_fma) *factor_fma = f;
+        if (solve_fma) *solve_fma = (long long)n * (n - 1) / 2;
+        if (factor_entries) *factor_entries = n * n;
+        return NNET_SUCCESS;
+    }
+    const int *rbeg, *rspec, *rcnt, *pbeg, *pspec, *pcnt;
+    if (network == 14)
+        rbeg = net14_reactant_begin, rspec = net14_reactant_species, rcnt = net14_reactant_count,
+        pbeg = net14_product_begin, pspec = net14_product_species, pcnt = net14_product_count;
+    else if (network == 86)
+        rbeg = net86_reactant_begin, rspec = net86_reactant_species, rcnt = net86_reactant_count,
+        pbeg = net86_product_begin, pspec = net86_product_species, pcnt = net86_product_count;
+    else
+        rbeg = net87_reactant_begin, rspec = net87_reactant_species, rcnt = net87_reactant_count,
+        pbeg = net87_product_begin, pspec = net87_product_species, pcnt = net87_product_count;
+    const SparsePlan p = buildSparsePlan(network, rbeg, rspec, rcnt, pbeg, pspec, pcnt, R);
+    if (factor_fma) *factor_fma = p.factorFma;
+    if (solve_fma) *solve_fma = p.solveFma;
+    if (factor_entries) *factor_entries = p.nnz;
     return NNET_SUCCESS;
 }
 
@@ -205,12 +221,11 @@ int nnet_create(int device, nnet_handle* out)
             return rc;
         }
     }
-    if (cudaMalloc(&h->counters, kCounters * sizeof(unsigned long long)) != cudaSuccess)
+    if (int rc = h->ws.ensure(0, nullptr))
     {
         nnet_destroy(h);
-        return fail(NNET_ERR_CUDA, "cudaMalloc counters");
+        return rc;
     }
-    cudaMemset(h->counters, 0, kCounters * sizeof(unsigned long long));
     *out = h;
     return NNET_SUCCESS;
 }
@@ -223,8 +238,7 @@ int nnet_destroy(nnet_handle h)
     for (auto& n : h->nets)
         if (n.mem) cudaFree(n.mem);
     if (h->helmMem) cudaFree(h->helmMem);
-    if (h->scratch) cudaFree(h->scratch);
-    if (h->counters) cudaFree(h->counters);
+    h->ws.release();
     delete h;
     return NNET_SUCCESS;
 }
@@ -314,6 +328,58 @@ int nnet_load_helmholtz_table_file(nnet_handle h, const char* path)
 
 int nnet_burn(nnet_handle h, const nnet_burn_args* a, void* stream)
 {
+    if (!h) return fail(NNET_ERR_INVALID, "null argument");
+    const int rc = nnet_gb300::launchBurn(h, a, h->ws, (cudaStream_t)stream, nullptr, 0, nullptr);
+    if (rc == NNET_SUCCESS) h->lastStream = (cudaStream_t)stream;
+    return rc;
+}
+
+} // extern "C"
+
+int nnet_gb300::Workspace::ensure(size_t need, cudaStream_t st)
+{
+    if (!counters)
+    {
+        NNET_CUDA(cudaMalloc(&counters, kCounters * sizeof(unsigned long long)));
+        NNET_CUDA(cudaMemset(counters, 0, kCounters * sizeof(unsigned long long)));
+    }
+    if (need > doubles)
+    {
+        // grown, never shrunk (as the reference's devData.buffer, parallel_nuclear_net.cu:148)
+        NNET_CUDA(cudaStreamSynchronize(st));
+        if (scratch) cudaFree(scratch);
+        scratch = nullptr, doubles = 0;
+        NNET_CUDA(cudaMalloc(&scratch, need * sizeof(double)));
+        doubles = need;
+    }
+    return NNET_SUCCESS;
+}
+
+void nnet_gb300::Workspace::release()
+{
+    if (scratch) cudaFree(scratch);
+    if (counters) cudaFree(counters);
+    scratch = nullptr, counters = nullptr, doubles = 0;
+}
+
+size_t nnet_gb300::maxScratchDoubles(nnet_context* h, int solver)
+{
+    size_t m = 0;
+    for (int net : {14, 86, 87})
+        for (int eos : {0, 1})
+        {
+            KernelInfo ki = solver == NNET_SOLVER_DENSE_FP64 ? denseKernel(net, eos)
+                                                             : sparseKernel(net, eos, solver == NNET_SOLVER_MIXED);
+            int perSM = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, ki.func, ki.block, 0) != cudaSuccess) perSM = 1;
+            m = std::max(m, (size_t)h->numSMs * std::max(perSM, 1) * ki.block * ki.perSlot);
+        }
+    return m;
+}
+
+int nnet_gb300::launchBurn(nnet_context* h, const nnet_burn_args* a, Workspace& ws, cudaStream_t st,
+                           const ResumeState* rs, long long sliceIters, unsigned long long* segFinished)
+{
     if (!h || !a) return fail(NNET_ERR_INVALID, "null argument");
     const int ni = netIndex(a->network);
     if (ni < 0) return fail(NNET_ERR_INVALID, "unknown network");
@@ -326,7 +392,6 @@ int nnet_burn(nnet_handle h, const nnet_burn_args* a, void* stream)
     if (!(a->hydro_dt > 0)) return fail(NNET_ERR_INVALID, "hydro_dt must be > 0");
     if (a->use_drhodt && !(a->previous_dt != 0)) return fail(NNET_ERR_INVALID, "use_drhodt needs previous_dt != 0");
     NNET_CUDA(cudaSetDevice(h->device));
-    cudaStream_t st = (cudaStream_t)stream;
 
     KernelInfo ki;
     if (a->solver == NNET_SOLVER_DENSE_FP64)
@@ -346,17 +411,8 @@ int nnet_burn(nnet_handle h, const nnet_burn_args* a, void* stream)
     const size_t need      = (a->num_particles + ki.block - 1) / ki.block;
     const size_t blocks    = need < maxBlocks ? need : maxBlocks;
     const size_t slots     = blocks * ki.block;
-    const size_t doubles   = slots * ki.perSlot;
-    if (doubles > h->scratchDoubles)
-    {
-        // grown, never shrunk (as the reference's devData.buffer, parallel_nuclear_net.cu:148)
-        NNET_CUDA(cudaStreamSynchronize(st));
-        if (h->scratch) cudaFree(h->scratch);
-        h->scratch        = nullptr;
-        h->scratchDoubles = 0;
-        NNET_CUDA(cudaMalloc(&h->scratch, doubles * sizeof(double)));
-        h->scratchDoubles = doubles;
-    }
+    const int    wrc       = ws.ensure(slots * ki.perSlot, st);
+    if (wrc) return wrc;
 
     BurnParams bp{};
     bp.P = a->num_particles;
@@ -370,18 +426,21 @@ int nnet_burn(nnet_handle h, const nnet_burn_args* a, void* stream)
     bp.useDrhodt = a->use_drhodt && a->rho_m1;
     bp.maxIter   = a->max_newton_iterations > 0 ? a->max_newton_iterations : 100000;
     bp.status = a->status, bp.substeps = a->substeps, bp.iterations = a->iterations;
-    bp.queue = h->counters, bp.stats = h->counters + 1, bp.order = nullptr;
+    bp.queue = ws.counters, bp.stats = ws.counters + 1, bp.order = nullptr;
+    if (rs) bp.rs = *rs;
+    bp.sliceIters = sliceIters, bp.segOf = nullptr, bp.segFinished = segFinished;
 
-    NNET_CUDA(cudaMemsetAsync(h->counters, 0, kCounters * sizeof(unsigned long long), st));
+    NNET_CUDA(cudaMemsetAsync(ws.counters, 0, kCounters * sizeof(unsigned long long), st));
     NetView  nv     = h->nets[ni].view;
     HelmView hv     = h->helm;
-    double*  sc     = h->scratch;
+    double*  sc     = ws.scratch;
     size_t   stride = slots;
     void*    args[] = {&bp, &nv, &hv, &sc, &stride};
     NNET_CUDA(cudaLaunchKernel(ki.func, dim3((unsigned)blocks), dim3(ki.block), args, 0, st));
-    h->lastStream = st;
     return NNET_SUCCESS;
 }
+
+extern "C" {
 
 int nnet_get_stats(nnet_handle h, nnet_stats* out)
 {
@@ -389,7 +448,7 @@ int nnet_get_stats(nnet_handle h, nnet_stats* out)
     NNET_CUDA(cudaSetDevice(h->device));
     NNET_CUDA(cudaStreamSynchronize(h->lastStream));
     unsigned long long v[kCounters];
-    NNET_CUDA(cudaMemcpy(v, h->counters, sizeof v, cudaMemcpyDeviceToHost));
+    NNET_CUDA(cudaMemcpy(v, h->ws.counters, sizeof v, cudaMemcpyDeviceToHost));
     out->newton_iterations = v[1];
     out->substeps          = v[2];
     for (int s = 0; s < 5; ++s)

@@ -86,6 +86,18 @@ enum : int32_t
     ST_ZERO_DT  = NNET_PARTICLE_ZERO_DT,
 };
 
+// Per-particle state that lets a burn pause at an attempt boundary and resume later with
+// bit-identical arithmetic (continuous batching).  phase: 0 not started, 1 paused,
+// 2 finished.  Y, T and dt live in the particle arrays themselves.
+struct ResumeState
+{
+    int*                phase;
+    double *            elapsed, *nextT, *drho;
+    long long*          nit;
+    int *               nsub, *cdPower, *cdSteps;
+    unsigned long long *cdDt, *cdNt;
+};
+
 // Batch arguments as seen by the kernels
 struct BurnParams
 {
@@ -105,6 +117,13 @@ struct BurnParams
     unsigned long long* stats;  // [0] Newton iterations, [1] substeps, [2+s] status counts,
                                 // [7] refinement steps, [8] FP64 fallbacks
     const uint32_t*     order;  // optional particle visiting order (nullptr: identity)
+    // continuous batching (all optional): resumable state, Newton-iteration budget of this
+    // launch per particle (a particle pauses at the first attempt boundary past it), and a
+    // per-particle segment id whose finished-particle counter is incremented on completion
+    ResumeState         rs;
+    long long           sliceIters;
+    const int*          segOf;
+    unsigned long long* segFinished;
 };
 
 } // namespace nnet_gb300

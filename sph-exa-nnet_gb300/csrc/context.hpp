@@ -1,0 +1,51 @@
+// Library context (the object behind nnet_handle) and the internal burn launcher shared by
+// the C ABI and the burn server.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+#include "sparse_plan.hpp"
+
+namespace nnet_gb300
+{
+
+// one device allocation per network holding every table of NetView
+struct NetBuffer
+{
+    void*      mem = nullptr;
+    NetView    view{};
+    SparsePlan plan;
+};
+
+// per-launch resources: the persistent grid's slot scratch and the queue / stats counters.
+// One launch may be in flight per workspace.
+struct Workspace
+{
+    double*             scratch  = nullptr;
+    size_t              doubles  = 0;
+    unsigned long long* counters = nullptr; // [0] queue head, [1..] stats (BurnParams::stats)
+    int                 ensure(size_t need, cudaStream_t st);
+    void                release();
+};
+
+// Launch one burn over args->num_particles particles on `st` with workspace `ws`.
+// rs / sliceIters / segFinished enable pausing and resuming (see BurnParams).
+int launchBurn(struct ::nnet_context* h, const nnet_burn_args* args, Workspace& ws, cudaStream_t st,
+               const ResumeState* rs, long long sliceIters, unsigned long long* segFinished);
+
+// scratch doubles of the largest persistent grid of any network for `solver`
+size_t maxScratchDoubles(struct ::nnet_context* h, int solver);
+
+} // namespace nnet_gb300
+
+struct nnet_context
+{
+    int                    device = 0, numSMs = 0;
+    nnet_gb300::NetBuffer  nets[3];
+    void*                  helmMem    = nullptr;
+    nnet_gb300::HelmView   helm{};
+    bool                   helmLoaded = false;
+    nnet_gb300::Workspace  ws;
+    cudaStream_t           lastStream = nullptr;
+};

@@ -27,7 +27,7 @@ struct ParticleState
 {
     size_t             p;
     double             T, dt, elapsed, nextT, rho, drho;
-    long long          nit;
+    long long          nit, nit0; // Newton iterations so far / at the start of this launch
     int                i, nsub;
     unsigned long long cdDt, cdNt; // cycle detection: saved attempt-start state (bits)
     int                cdPower, cdSteps;
@@ -81,6 +81,12 @@ __device__ __forceinline__ void networkRates(const NetView& nv, Strided<double> 
 
 // Fetch the next burnable particle; skipped ones (rho <= 1e5 or T <= 1e8,
 // parallel_nuclear_net_impl.cpp:83) are written back immediately.
+__device__ __forceinline__ void finishSegment(const BurnParams& bp, size_t p)
+{
+    if (bp.rs.phase) bp.rs.phase[p] = 2;
+    if (bp.segFinished) atomicAdd(bp.segFinished + (bp.segOf ? bp.segOf[p] : 0), 1ull);
+}
+
 template<int NET, class Policy>
 __device__ bool acquire(const BurnParams& bp, Policy& pol, ParticleState& s)
 {
@@ -88,41 +94,77 @@ __device__ bool acquire(const BurnParams& bp, Policy& pol, ParticleState& s)
     {
         unsigned long long q = atomicAdd(bp.queue, 1ull);
         if (q >= bp.P) return false;
-        const size_t p   = bp.order ? (size_t)bp.order[q] : (size_t)q;
+        const size_t p     = bp.order ? (size_t)bp.order[q] : (size_t)q;
+        const int    phase = bp.rs.phase ? bp.rs.phase[p] : 0;
+        if (phase == 2) continue; // finished in an earlier launch
         const double rho = bp.rho[p], T = bp.T[p];
-        if (!(rho > k::minRho && T > k::minTemp))
+        if (phase == 0 && !(rho > k::minRho && T > k::minTemp))
         {
             if (bp.status) bp.status[p] = ST_SKIPPED;
             if (bp.substeps) bp.substeps[p] = 0;
             if (bp.iterations) bp.iterations[p] = 0;
             atomicAdd(bp.stats + 2 + ST_SKIPPED, 1ull);
+            finishSegment(bp, p);
             continue;
         }
         for (int j = 0; j < NET; ++j)
             pol.Y[j] = bp.Y[j][p];
-        double drho = 0;
-        if (bp.useDrhodt && bp.rhoM1 && bp.rhoM1[p] != 0) drho = (rho - bp.rhoM1[p]) / bp.previousDt;
-        s.p = p, s.T = T, s.dt = bp.dt[p], s.elapsed = 0, s.nextT = 0;
-        s.rho = rho, s.drho = drho, s.nit = 0, s.i = 1, s.nsub = 0;
-        s.cycleReset();
+        s.p = p, s.T = T, s.dt = bp.dt[p], s.rho = rho, s.i = 1;
+        if (phase == 1)
+        {
+            const ResumeState& r = bp.rs;
+            s.elapsed = r.elapsed[p], s.nextT = r.nextT[p], s.drho = r.drho[p], s.nit = r.nit[p];
+            s.nsub = r.nsub[p], s.cdDt = r.cdDt[p], s.cdNt = r.cdNt[p], s.cdPower = r.cdPower[p];
+            s.cdSteps = r.cdSteps[p];
+        }
+        else
+        {
+            double drho = 0;
+            if (bp.useDrhodt && bp.rhoM1 && bp.rhoM1[p] != 0) drho = (rho - bp.rhoM1[p]) / bp.previousDt;
+            s.elapsed = 0, s.nextT = 0, s.drho = drho, s.nit = 0, s.nsub = 0;
+            s.cycleReset();
+        }
+        s.nit0 = s.nit;
         return true;
     }
 }
 
 template<int NET, class Policy>
-__device__ void release(const BurnParams& bp, Policy& pol, const ParticleState& s, int status)
+__device__ void writeState(const BurnParams& bp, Policy& pol, const ParticleState& s)
 {
     for (int j = 0; j < NET; ++j)
         bp.Y[j][s.p] = pol.Y[j];
     bp.T[s.p]  = s.T;
     bp.dt[s.p] = s.dt;
+}
+
+template<int NET, class Policy>
+__device__ void release(const BurnParams& bp, Policy& pol, const ParticleState& s, int status)
+{
+    writeState<NET>(bp, pol, s);
     if (bp.status) bp.status[s.p] = status;
     if (bp.substeps) bp.substeps[s.p] = s.nsub;
     if (bp.iterations) bp.iterations[s.p] = (int32_t)s.nit;
-    atomicAdd(bp.stats + 0, (unsigned long long)s.nit);
+    atomicAdd(bp.stats + 0, (unsigned long long)(s.nit - s.nit0));
     atomicAdd(bp.stats + 1, (unsigned long long)s.nsub);
     atomicAdd(bp.stats + 2 + status, 1ull);
+    finishSegment(bp, s.p);
 }
+
+// pause at an attempt boundary: everything the next attempt depends on is saved
+template<int NET, class Policy>
+__device__ void pause(const BurnParams& bp, Policy& pol, const ParticleState& s)
+{
+    writeState<NET>(bp, pol, s);
+    const ResumeState& r = bp.rs;
+    const size_t       p = s.p;
+    r.elapsed[p] = s.elapsed, r.nextT[p] = s.nextT, r.drho[p] = s.drho, r.nit[p] = s.nit, r.nsub[p] = s.nsub;
+    r.cdDt[p] = s.cdDt, r.cdNt[p] = s.cdNt, r.cdPower[p] = s.cdPower, r.cdSteps[p] = s.cdSteps;
+    r.phase[p] = 1;
+    atomicAdd(bp.stats + 0, (unsigned long long)(s.nit - s.nit0));
+}
+
+constexpr int kPaused = -2;
 
 // One Newton iteration of the substep loop.  Returns -1 to continue, or the particle's
 // final status.
@@ -131,6 +173,7 @@ __device__ int newtonIteration(const BurnParams& bp, const NetView& nv, const He
                                ParticleState& s)
 {
     if (s.nit >= bp.maxIter) return ST_MAXITER;
+    if (bp.sliceIters > 0 && s.i == 1 && s.nit - s.nit0 >= bp.sliceIters) return kPaused;
 
     // prepareSystemSubstep (nuclear_net.hpp:858-879)
     const double dtTot = bp.hydroDt;
@@ -245,6 +288,11 @@ __device__ __forceinline__ void burnLoop(const BurnParams& bp, const NetView& nv
         if (st >= 0)
         {
             release<NET>(bp, pol, s, st);
+            have = acquire<NET>(bp, pol, s);
+        }
+        else if (st == kPaused)
+        {
+            pause<NET>(bp, pol, s);
             have = acquire<NET>(bp, pol, s);
         }
     }

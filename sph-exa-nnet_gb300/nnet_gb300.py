@@ -75,6 +75,9 @@ def load_library(path=LIB_PATH):
     lib.nnet_helmholtz_eos.argtypes = [P, S, I, P, P, P, P, P, P, P, P, P, P]
     lib.nnet_network_info.argtypes = [I, ctypes.POINTER(I), ctypes.POINTER(I)]
     lib.nnet_last_error_message.restype = ctypes.c_char_p
+    lib.nnet_solver_info.argtypes = [I, I, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong),
+                                     ctypes.POINTER(I)]
+    lib.nnet_measure_fp64_peak.argtypes = [I, ctypes.POINTER(D)]
     _lib = lib
     return lib
 
@@ -240,6 +243,24 @@ def compute_nuclear_reactions(n, first, last, hydro_dt, previous_dt, reactions, 
              solver=solver, status=None if status is None else status[sl], max_iter=max_iter, **kw)
 
 
+def solver_info(network, solver):
+    """(factorisation FMAs, triangular-solve FMAs, stored factor entries) of one Newton solve."""
+    lib = load_library()
+    if isinstance(solver, str):
+        solver = SOLVERS[solver]
+    f, s, e = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_int()
+    _check(lib.nnet_solver_info(network, solver, ctypes.byref(f), ctypes.byref(s), ctypes.byref(e)))
+    return f.value, s.value, e.value
+
+
+def measure_fp64_peak(device=0):
+    """FP64 FMA throughput of the device in TFLOP/s (dependency-free probe kernel)."""
+    lib = load_library()
+    t = ctypes.c_double()
+    _check(lib.nnet_measure_fp64_peak(device, ctypes.byref(t)))
+    return t.value
+
+
 def network_charges(network):
     """Z of a network's species (net87 includes the electron entry, Z = -1)."""
     import re
@@ -256,3 +277,83 @@ def compute_helm_eos(n, first, last, Z, context=None):
     sl = slice(first, last)
     ctx.helmholtz_eos(Z, n.temp[sl], n.rho[sl], [y[sl] for y in n.Y], n.u[sl], n.cv[sl], n.p[sl], n.c[sl],
                       n.dpdT[sl])
+
+
+# ---------------------------------------------------------------- burn server
+class _ServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_double), ("solver", ctypes.c_int),
+                ("slice_iterations", ctypes.c_longlong), ("max_concurrent_requests", ctypes.c_int)]
+
+
+class _Request(ctypes.Structure):
+    _fields_ = [("network", ctypes.c_int), ("eos", ctypes.c_int), ("ideal_gas_mu", ctypes.c_double),
+                ("num_particles", ctypes.c_size_t), ("Y", ctypes.c_void_p), ("T", ctypes.c_void_p),
+                ("rho", ctypes.c_void_p), ("dt", ctypes.c_void_p), ("status", ctypes.c_void_p),
+                ("hydro_dt", ctypes.c_double), ("max_newton_iterations", ctypes.c_longlong)]
+
+
+class _ServerStats(ctypes.Structure):
+    _fields_ = [("completed_requests", ctypes.c_ulonglong), ("completed_particles", ctypes.c_double),
+                ("span_seconds", ctypes.c_double), ("latency_p50", ctypes.c_double),
+                ("latency_p95", ctypes.c_double), ("latency_p99", ctypes.c_double),
+                ("latency_max", ctypes.c_double), ("slices", ctypes.c_ulonglong)]
+
+
+class Server:
+    """Continuous-batching burn server over the C ABI (nnet_server_*).  Requests carry
+    host numpy arrays (float64; Y species-major [network, P]); results overwrite them."""
+
+    def __init__(self, context, solver=SOLVER_MIXED, hbm_budget_bytes=150e9, slice_iterations=64,
+                 max_concurrent_requests=8):
+        lib = load_library()
+        P = ctypes.c_void_p
+        lib.nnet_server_create.argtypes = [P, ctypes.POINTER(_ServerConfig), ctypes.POINTER(P)]
+        lib.nnet_server_submit.argtypes = [P, ctypes.POINTER(_Request), ctypes.POINTER(ctypes.c_uint64)]
+        lib.nnet_server_query.argtypes = [P, ctypes.c_uint64, ctypes.POINTER(ctypes.c_int)]
+        lib.nnet_server_wait.argtypes = [P, ctypes.c_uint64, ctypes.POINTER(ctypes.c_double)]
+        lib.nnet_server_get_stats.argtypes = [P, ctypes.POINTER(_ServerStats)]
+        lib.nnet_server_destroy.argtypes = [P]
+        if isinstance(solver, str):
+            solver = SOLVERS[solver]
+        cfg = _ServerConfig(hbm_budget_bytes, solver, slice_iterations, max_concurrent_requests)
+        s = ctypes.c_void_p()
+        rc = lib.nnet_server_create(context.handle, ctypes.byref(cfg), ctypes.byref(s))
+        if rc != 0:
+            raise NnetError(f"nnet_server_create failed ({rc})")
+        self.handle, self.context, self._keep = s, context, {}
+
+    def submit(self, network, Y, T, rho, dt, hydro_dt, eos=EOS_HELMHOLTZ, mu=0.0, status=None, max_iter=100000):
+        if isinstance(eos, str):
+            eos = EOS_IDEAL_GAS if eos.startswith("ideal") else EOS_HELMHOLTZ
+        for a in (Y, T, rho, dt):
+            if a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"]:
+                raise NnetError("request arrays must be C-contiguous float64")
+        r = _Request(network, eos, mu, T.size, Y.ctypes.data, T.ctypes.data, rho.ctypes.data, dt.ctypes.data,
+                     None if status is None else status.ctypes.data, hydro_dt, max_iter)
+        rid = ctypes.c_uint64()
+        _check(_lib.nnet_server_submit(self.handle, ctypes.byref(r), ctypes.byref(rid)))
+        self._keep[rid.value] = (Y, T, rho, dt, status)
+        return rid.value
+
+    def done(self, rid):
+        d = ctypes.c_int()
+        _check(_lib.nnet_server_query(self.handle, rid, ctypes.byref(d)))
+        return d.value
+
+    def wait(self, rid):
+        lat = ctypes.c_double()
+        rc = _lib.nnet_server_wait(self.handle, rid, ctypes.byref(lat))
+        self._keep.pop(rid, None)
+        if rc != 0:
+            raise NnetError(f"request {rid} failed")
+        return lat.value
+
+    def stats(self):
+        st = _ServerStats()
+        _check(_lib.nnet_server_get_stats(self.handle, ctypes.byref(st)))
+        return {k: getattr(st, k) for k, _ in _ServerStats._fields_}
+
+    def close(self):
+        if self.handle:
+            _lib.nnet_server_destroy(self.handle)
+            self.handle = None

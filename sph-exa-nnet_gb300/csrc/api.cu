@@ -14,6 +14,7 @@
 #include "launch.hpp"
 #include "sparse_plan.hpp"
 #include "context.hpp"
+#include "burn_multi.hpp"
 
 using namespace nnet_gb300;
 
@@ -124,7 +125,8 @@ int uploadNetwork(int net, NetBuffer& b)
     return NNET_SUCCESS;
 }
 
-constexpr int kCounters = 16;
+constexpr int kNetCounters = 16;             // queue head + stats of one launch
+constexpr int kCounters    = 4 * kNetCounters; // single launch uses [0, 16); a batch one region per network
 
 int netIndex(int net) { return net == 14 ? 0 : net == 86 ? 1 : net == 87 ? 2 : -1; }
 
@@ -330,7 +332,7 @@ int nnet_burn(nnet_handle h, const nnet_burn_args* a, void* stream)
 {
     if (!h) return fail(NNET_ERR_INVALID, "null argument");
     const int rc = nnet_gb300::launchBurn(h, a, h->ws, (cudaStream_t)stream, nullptr, 0, nullptr);
-    if (rc == NNET_SUCCESS) h->lastStream = (cudaStream_t)stream;
+    if (rc == NNET_SUCCESS) h->lastStream = (cudaStream_t)stream, h->lastMulti = false;
     return rc;
 }
 
@@ -377,56 +379,71 @@ size_t nnet_gb300::maxScratchDoubles(nnet_context* h, int solver)
     return m;
 }
 
-int nnet_gb300::launchBurn(nnet_context* h, const nnet_burn_args* a, Workspace& ws, cudaStream_t st,
-                           const ResumeState* rs, long long sliceIters, unsigned long long* segFinished)
+namespace
+{
+int validate(nnet_context* h, const nnet_burn_args* a)
 {
     if (!h || !a) return fail(NNET_ERR_INVALID, "null argument");
-    const int ni = netIndex(a->network);
-    if (ni < 0) return fail(NNET_ERR_INVALID, "unknown network");
+    if (netIndex(a->network) < 0) return fail(NNET_ERR_INVALID, "unknown network");
     if (a->eos != NNET_EOS_IDEAL_GAS && a->eos != NNET_EOS_HELMHOLTZ) return fail(NNET_ERR_INVALID, "unknown eos");
     if (a->eos == NNET_EOS_HELMHOLTZ && !h->helmLoaded)
         return fail(NNET_ERR_NO_TABLE, "Helmholtz EOS requested before nnet_load_helmholtz_table");
     if (a->eos == NNET_EOS_IDEAL_GAS && !(a->ideal_gas_mu > 0)) return fail(NNET_ERR_INVALID, "ideal_gas_mu must be > 0");
+    if (a->solver < NNET_SOLVER_DENSE_FP64 || a->solver > NNET_SOLVER_MIXED) return fail(NNET_ERR_INVALID, "unknown solver");
     if (a->num_particles == 0) return NNET_SUCCESS;
     if (!a->Y || !a->T || !a->rho || !a->dt) return fail(NNET_ERR_INVALID, "null particle array");
+    for (int j = 0; j < a->network; ++j)
+        if (!a->Y[j]) return fail(NNET_ERR_INVALID, "null species pointer");
     if (!(a->hydro_dt > 0)) return fail(NNET_ERR_INVALID, "hydro_dt must be > 0");
     if (a->use_drhodt && !(a->previous_dt != 0)) return fail(NNET_ERR_INVALID, "use_drhodt needs previous_dt != 0");
-    NNET_CUDA(cudaSetDevice(h->device));
+    return NNET_SUCCESS;
+}
 
-    KernelInfo ki;
-    if (a->solver == NNET_SOLVER_DENSE_FP64)
-        ki = denseKernel(a->network, a->eos);
-    else if (a->solver == NNET_SOLVER_SPARSE_FP64 || a->solver == NNET_SOLVER_MIXED)
-        ki = sparseKernel(a->network, a->eos, a->solver == NNET_SOLVER_MIXED);
-    else
-        return fail(NNET_ERR_INVALID, "unknown solver");
-    if (!ki.func) return fail(NNET_ERR_INVALID, "solver not available for this network");
-    if (ki.maxNnz && h->nets[ni].plan.nnz > ki.maxNnz)
-        return fail(NNET_ERR_TOO_LARGE, "sparse factor does not fit the kernel's storage");
-
-    int perSM = 0;
-    NNET_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, ki.func, ki.block, 0));
-    if (perSM < 1) perSM = 1;
-    const size_t maxBlocks = (size_t)h->numSMs * perSM;
-    const size_t need      = (a->num_particles + ki.block - 1) / ki.block;
-    const size_t blocks    = need < maxBlocks ? need : maxBlocks;
-    const size_t slots     = blocks * ki.block;
-    const int    wrc       = ws.ensure(slots * ki.perSlot, st);
-    if (wrc) return wrc;
-
-    BurnParams bp{};
+void fillParams(const nnet_burn_args* a, unsigned long long* counters, BurnParams& bp)
+{
+    bp   = BurnParams{};
     bp.P = a->num_particles;
     for (int j = 0; j < a->network; ++j)
-    {
-        if (!a->Y[j]) return fail(NNET_ERR_INVALID, "null species pointer");
         bp.Y[j] = a->Y[j];
-    }
     bp.T = a->T, bp.rho = a->rho, bp.rhoM1 = a->rho_m1, bp.dt = a->dt;
     bp.hydroDt = a->hydro_dt, bp.previousDt = a->previous_dt, bp.mu = a->ideal_gas_mu;
     bp.useDrhodt = a->use_drhodt && a->rho_m1;
     bp.maxIter   = a->max_newton_iterations > 0 ? a->max_newton_iterations : 100000;
     bp.status = a->status, bp.substeps = a->substeps, bp.iterations = a->iterations;
-    bp.queue = ws.counters, bp.stats = ws.counters + 1, bp.order = nullptr;
+    bp.queue = counters, bp.stats = counters + 1, bp.order = nullptr;
+}
+
+// persistent grid of `ki` for P particles: (blocks, slots)
+int gridFor(nnet_context* h, const KernelInfo& ki, size_t P, size_t& blocks, size_t& slots)
+{
+    int perSM = 0;
+    NNET_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, ki.func, ki.block, 0));
+    if (perSM < 1) perSM = 1;
+    const size_t maxBlocks = (size_t)h->numSMs * perSM;
+    const size_t need      = (P + ki.block - 1) / ki.block;
+    blocks                 = need < maxBlocks ? need : maxBlocks;
+    slots                  = blocks * ki.block;
+    return NNET_SUCCESS;
+}
+} // namespace
+
+int nnet_gb300::launchBurn(nnet_context* h, const nnet_burn_args* a, Workspace& ws, cudaStream_t st,
+                           const ResumeState* rs, long long sliceIters, unsigned long long* segFinished)
+{
+    if (int rc = validate(h, a)) return rc;
+    if (a->num_particles == 0) return NNET_SUCCESS;
+    NNET_CUDA(cudaSetDevice(h->device));
+    const int  ni = netIndex(a->network);
+    KernelInfo ki = a->solver == NNET_SOLVER_DENSE_FP64 ? denseKernel(a->network, a->eos)
+                                                        : sparseKernel(a->network, a->eos, a->solver == NNET_SOLVER_MIXED);
+    if (ki.maxNnz && h->nets[ni].plan.nnz > ki.maxNnz)
+        return fail(NNET_ERR_TOO_LARGE, "sparse factor does not fit the kernel's storage");
+    size_t blocks, slots;
+    if (int rc = gridFor(h, ki, a->num_particles, blocks, slots)) return rc;
+    if (int rc = ws.ensure(slots * ki.perSlot, st)) return rc;
+
+    BurnParams bp;
+    fillParams(a, ws.counters, bp);
     if (rs) bp.rs = *rs;
     bp.sliceIters = sliceIters, bp.segOf = nullptr, bp.segFinished = segFinished;
 
@@ -440,6 +457,49 @@ int nnet_gb300::launchBurn(nnet_context* h, const nnet_burn_args* a, Workspace& 
     return NNET_SUCCESS;
 }
 
+extern "C" int nnet_burn_batch(nnet_handle h, const nnet_burn_args* batches, int count, void* stream)
+{
+    if (!h || !batches || count < 1 || count > 3) return fail(NNET_ERR_INVALID, "need 1 to 3 sub-batches");
+    MultiParams mp{};
+    size_t      total = 0;
+    for (int k = 0; k < count; ++k)
+    {
+        const nnet_burn_args* a = batches + k;
+        if (int rc = validate(h, a)) return rc;
+        if (a->eos != batches[0].eos || a->solver != batches[0].solver)
+            return fail(NNET_ERR_INVALID, "sub-batches must share the EOS and the solver");
+        const int ni = netIndex(a->network);
+        if (mp.active[ni]) return fail(NNET_ERR_INVALID, "at most one sub-batch per network");
+        mp.active[ni] = a->num_particles > 0;
+        mp.nv[ni]     = h->nets[ni].view;
+        total += a->num_particles;
+    }
+    if (total == 0) return NNET_SUCCESS;
+    NNET_CUDA(cudaSetDevice(h->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    KernelInfo   ki = multiKernel(batches[0].eos, batches[0].solver);
+    for (int ni = 0; ni < 3; ++ni)
+        if (mp.active[ni] && ki.maxNnz && h->nets[ni].plan.nnz > ki.maxNnz)
+            return fail(NNET_ERR_TOO_LARGE, "sparse factor does not fit the kernel's storage");
+    size_t blocks, slots;
+    if (int rc = gridFor(h, ki, total, blocks, slots)) return rc;
+    if (int rc = h->ws.ensure(slots * ki.perSlot, st)) return rc;
+    for (int k = 0; k < count; ++k)
+    {
+        const int ni = netIndex(batches[k].network);
+        fillParams(batches + k, h->ws.counters + kNetCounters * (ni + 1), mp.bp[ni]);
+    }
+    NNET_CUDA(cudaMemsetAsync(h->ws.counters, 0, kCounters * sizeof(unsigned long long), st));
+    HelmView hv     = h->helm;
+    double*  sc     = h->ws.scratch;
+    size_t   stride = slots;
+    void*    args[] = {&mp, &hv, &sc, &stride};
+    NNET_CUDA(cudaLaunchKernel(ki.func, dim3((unsigned)blocks), dim3(ki.block), args, 0, st));
+    h->lastStream = st;
+    h->lastMulti  = true;
+    return NNET_SUCCESS;
+}
+
 extern "C" {
 
 int nnet_get_stats(nnet_handle h, nnet_stats* out)
@@ -447,8 +507,11 @@ int nnet_get_stats(nnet_handle h, nnet_stats* out)
     if (!h || !out) return fail(NNET_ERR_INVALID, "null argument");
     NNET_CUDA(cudaSetDevice(h->device));
     NNET_CUDA(cudaStreamSynchronize(h->lastStream));
-    unsigned long long v[kCounters];
-    NNET_CUDA(cudaMemcpy(v, h->ws.counters, sizeof v, cudaMemcpyDeviceToHost));
+    unsigned long long all[kCounters], v[kNetCounters] = {};
+    NNET_CUDA(cudaMemcpy(all, h->ws.counters, sizeof all, cudaMemcpyDeviceToHost));
+    for (int r = h->lastMulti ? 1 : 0; r < (h->lastMulti ? 4 : 1); ++r)
+        for (int k = 0; k < kNetCounters; ++k)
+            v[k] += all[r * kNetCounters + k];
     out->newton_iterations = v[1];
     out->substeps          = v[2];
     for (int s = 0; s < 5; ++s)

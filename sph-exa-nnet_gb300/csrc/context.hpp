@@ -48,4 +48,5 @@ struct nnet_context
     bool                   helmLoaded = false;
     nnet_gb300::Workspace  ws;
     cudaStream_t           lastStream = nullptr;
+    bool                   lastMulti  = false; // last launch was nnet_burn_batch
 };

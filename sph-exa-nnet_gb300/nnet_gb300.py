@@ -165,6 +165,32 @@ class Context:
         s = torch.cuda.current_stream(self.device) if stream is None else stream
         _check(_lib.nnet_burn(self.handle, ctypes.byref(a), ctypes.c_void_p(s.cuda_stream)))
 
+    def burn_batch(self, batches, solver=SOLVER_MIXED, eos=EOS_HELMHOLTZ, mu=0.0, max_iter=100000, stream=None):
+        """One launch over sub-batches of different networks.  `batches`: list of dicts with
+        keys network, Y, T, rho, dt, hydro_dt and optional status / iterations (CUDA tensors)."""
+        import torch
+        if isinstance(solver, str):
+            solver = SOLVERS[solver]
+        if isinstance(eos, str):
+            eos = EOS_IDEAL_GAS if eos.startswith("ideal") else EOS_HELMHOLTZ
+        arr = (_BurnArgs * len(batches))()
+        keep = []
+        for k, b in enumerate(batches):
+            net = b["network"]
+            yp = (ctypes.c_void_p * net)(*[b["Y"][j].data_ptr() for j in range(net)])
+            keep.append(yp)
+            st, it = b.get("status"), b.get("iterations")
+            arr[k] = _BurnArgs(network=net, eos=eos, ideal_gas_mu=mu, solver=solver, num_particles=b["T"].numel(),
+                               Y=ctypes.cast(yp, ctypes.POINTER(ctypes.c_void_p)), T=b["T"].data_ptr(),
+                               rho=b["rho"].data_ptr(), rho_m1=None, dt=b["dt"].data_ptr(), hydro_dt=b["hydro_dt"],
+                               previous_dt=0.0, use_drhodt=0, max_newton_iterations=max_iter,
+                               status=None if st is None else st.data_ptr(), substeps=None,
+                               iterations=None if it is None else it.data_ptr())
+        s = torch.cuda.current_stream(self.device) if stream is None else stream
+        lib = load_library()
+        lib.nnet_burn_batch.argtypes = [ctypes.c_void_p, ctypes.POINTER(_BurnArgs), ctypes.c_int, ctypes.c_void_p]
+        _check(lib.nnet_burn_batch(self.handle, arr, len(batches), ctypes.c_void_p(s.cuda_stream)))
+
     def stats(self):
         st = _Stats()
         _check(_lib.nnet_get_stats(self.handle, ctypes.byref(st)))

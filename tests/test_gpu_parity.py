@@ -157,3 +157,24 @@ def test_helmholtz_eos_batch(ctx, port):
         g = o.cpu().numpy()
         rel = np.abs(g - ref[name]) / np.abs(ref[name])
         assert rel.max() < 1e-12, (name, rel.max())
+
+
+@pytest.mark.parametrize("solver", ["mixed", "dense"])
+def test_mixed_network_single_launch(ctx, solver):
+    """c3-shaped mix in one launch equals separate per-network burns bit for bit."""
+    import torch
+    dev = torch.device("cuda:0")
+    parts = workloads.make_mixed(6000, 55)
+    one, sep = [], []
+    for w in parts:
+        one.append(dict(network=w["net"], Y=torch.tensor(w["Y"], device=dev), T=torch.tensor(w["T"], device=dev),
+                        rho=torch.tensor(w["rho"], device=dev), dt=torch.tensor(w["dt"], device=dev),
+                        hydro_dt=w["hydro_dt"], status=torch.zeros(w["T"].size, dtype=torch.int32, device=dev)))
+    ctx.burn_batch(one, solver=solver, max_iter=20000)
+    torch.cuda.synchronize()
+    st = ctx.stats()
+    assert sum(st["status"].values()) == 6000
+    for w, b in zip(parts, one):
+        g = gpu_burn(ctx, w, solver)
+        assert np.array_equal(b["Y"].cpu().numpy(), g[0]) and np.array_equal(b["T"].cpu().numpy(), g[1])
+        assert np.array_equal(b["status"].cpu().numpy(), g[3])

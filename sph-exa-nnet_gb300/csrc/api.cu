@@ -77,7 +77,15 @@ int uploadNetwork(int net, NetBuffer& b)
     std::vector<double> z53(N, 0.);
     for (int i = 0; i < N && i < (net == 14 ? 14 : 86); ++i)
         z53[i] = std::pow(Z[i], 5. / 3.); // host libm, as the reference's per-call pow(Z, 5/3)
+    std::vector<double> zf(4 * N, 0.);
+    for (int i = 0; i < N; ++i)
+    {
+        const double z = z53[i];
+        zf[4 * i + 0] = std::sqrt(z), zf[4 * i + 1] = std::sqrt(std::sqrt(z));
+        zf[4 * i + 2] = std::pow(z, 1.9885), zf[4 * i + 3] = z > 0 ? std::log(z) : 0.;
+    }
     const size_t oBE = putd(BE, N), oZ = putd(Z, net == 14 ? 14 : 87), oZ53 = putd(z53.data(), N);
+    const size_t oZf = putd(zf.data(), zf.size());
     const size_t oFit = putd(fit, nfit), oQ = putd(q, nq), oCh = putd(choose, nchoose);
     const size_t oLT = putd(net87_electron_log_temp, NET87_ELECTRON_NTEMP);
     const size_t oLR = putd(net87_electron_log_rho, NET87_ELECTRON_NRHO);
@@ -113,6 +121,7 @@ int uploadNetwork(int net, NetBuffer& b)
     v.net = net, v.nspec = N, v.nreact = R;
     v.rbeg = I + oRb, v.rspec = I + oRs, v.rcnt = I + oRc, v.pbeg = I + oPb, v.pspec = I + oPs, v.pcnt = I + oPc;
     v.BE = D + oBE, v.Z = D + oZ, v.z53 = D + oZ53, v.fit = D + oFit, v.q = D + oQ, v.choose = D + oCh;
+    v.zFac = D + oZf;
     v.mainReactant = I + oMr, v.secondaryReactant = I + oSr, v.mainProduct = I + oMp;
     v.eLogT = D + oLT, v.eLogRho = D + oLR, v.eRate = D + oER;
     SparseView& w = v.sp;

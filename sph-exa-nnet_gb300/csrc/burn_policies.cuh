@@ -23,6 +23,7 @@
 #pragma once
 
 #include "driver.cuh"
+#include "physics_fast.cuh"
 
 namespace nnet_gb300
 {
@@ -256,7 +257,7 @@ struct SparsePolicy
                              double dpdT, double dt)
     {
         const SparseView& sp = nv.sp;
-        networkRates<NET>(nv, Yn, Tg, rho, BE, rates, drates);
+        networkRatesFast<NET>(nv, Yn, Tg, rho, BE, rates, drates);
         for (int p = 0; p < sp.nnz; ++p)
             A[p] = 0.;
         for (int i = 0; i < D::N; ++i)

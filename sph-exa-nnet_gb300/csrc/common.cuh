@@ -60,6 +60,8 @@ struct NetView
     int           net, nspec, nreact;
     const int *   rbeg, *rspec, *rcnt, *pbeg, *pspec, *pcnt;
     const double *BE, *Z, *z53;
+    // per species i: sqrt(z53), sqrt(sqrt(z53)), z53^1.9885, log(z53) (fast rate forms)
+    const double* zFac;
     const double *fit, *q, *choose;
     const int *   mainReactant, *secondaryReactant, *mainProduct;
     const double *eLogT, *eLogRho, *eRate;

@@ -44,6 +44,10 @@ def parse():
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--cpu-sample", type=int, default=4096)
     ap.add_argument("--max-iter", type=int, default=20000)
+    ap.add_argument("--serve-requests", type=int, default=48,
+                    help="requests of the served-stream leg (0 disables it)")
+    ap.add_argument("--serve-plain-requests", type=int, default=12,
+                    help="requests of the plain-FP64 served-stream comparison (0 disables it)")
     return ap.parse_args()
 
 
@@ -166,7 +170,7 @@ def main():
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     ctx = nn.Context(local)
-    solver = args.solver or "dense"
+    solver = args.solver or "mixed"
     sv = nn.SOLVERS[solver]
 
     # ---- device-resident workload (this rank's shard)
@@ -286,6 +290,10 @@ def main():
             "kernel_ms": kernel_ms, "wall_s": wall, "clocks": clk.summary()}
     if plain:
         line["plain_fp64"] = plain
+    if args.serve_requests and rank == 0:
+        line["serving"] = serve_bench(nn, ctx, "mixed" if solver != "dense" else "dense", args.serve_requests, 5)
+        if args.serve_plain_requests and solver != "dense":
+            line["serving_plain_fp64"] = serve_bench(nn, ctx, "dense", args.serve_plain_requests, 5)
     if rank == 0:
         try:
             v, el, thr = cpu_burn_rate(args.cpu_sample)
@@ -297,6 +305,55 @@ def main():
     ctx.close()
     if world > 1:
         dist.destroy_process_group()
+
+
+def serve_requests(n, seed):
+    """Served burn stream: Poisson arrivals (mean 200/s), sizes log-uniform 1k-500k
+    particles, network tag uniform over net14/net86/net87, states drawn from the c2
+    (net86/net87 with Y_e = 0.5, net14 with the same composition) distributions."""
+    import workloads
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1 / 200.0, n)
+    sizes = np.exp(rng.uniform(np.log(1e3), np.log(5e5), n)).astype(int)
+    nets = rng.choice([14, 86, 87], n)
+    reqs = []
+    for k in range(n):
+        w = workloads.make("c2", P=int(sizes[k]), seed=seed * 1000 + k)
+        net = int(nets[k])
+        Y = workloads.composition(net, w["T"].size, 0.3, 0.7, 1e-10)
+        if net == 87:
+            Y[86] = 0.5
+        reqs.append(dict(net=net, Y=Y, T=w["T"], rho=w["rho"], dt=w["dt"], hydro_dt=w["hydro_dt"], gap=gaps[k]))
+    return reqs
+
+
+def serve_bench(nn, ctx, solver, n, seed):
+    """Submit the stream with its arrival gaps to a continuous-batching server (150 GB
+    HBM budget) and report served particle-burns/s and request latency percentiles."""
+    import torch
+    reqs = serve_requests(n, seed)
+    pinned = []
+    for r in reqs:  # pinned host buffers: asynchronous copies
+        arrs = [torch.from_numpy(np.ascontiguousarray(r[k])).pin_memory() for k in ("Y", "T", "rho", "dt")]
+        arrs.append(torch.zeros(r["T"].size, dtype=torch.int32).pin_memory())
+        pinned.append(arrs)
+    srv = nn.Server(ctx, solver=solver, hbm_budget_bytes=150e9, slice_iterations=64, max_concurrent_requests=8)
+    ids = []
+    t0 = time.perf_counter()
+    for r, a in zip(reqs, pinned):
+        time.sleep(r["gap"])
+        ids.append(srv.submit(r["net"], a[0].numpy(), a[1].numpy(), a[2].numpy(), a[3].numpy(), r["hydro_dt"],
+                              status=a[4].numpy(), max_iter=20000))
+    lat = [srv.wait(i) for i in ids]
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    particles = sum(r["T"].size for r in reqs)
+    return {"solver": solver, "requests": n, "particles": particles, "value": particles / wall, "unit": UNIT,
+            "wall_s": wall, "latency_p50_s": float(np.percentile(lat, 50)),
+            "latency_p95_s": float(np.percentile(lat, 95)), "latency_p99_s": float(np.percentile(lat, 99)),
+            "offered_load": "Poisson 200/s, sizes log-uniform 1e3-5e5, nets uniform {14,86,87}",
+            "slices": st["slices"]}
 
 
 def algorithmic_flops(nn, net, solver):

@@ -206,7 +206,10 @@ struct DensePolicy
 
 
 constexpr int    kMaxRefine = 3;
-constexpr double kRefineTol = 4e-16; // |d_k| <= tol |x_k| for every k ends the refinement
+// refinement ends when every correction is below kRefineTol of the component plus the
+// state it updates (|Y_j| for a species row, T for the temperature row), i.e. at FP64
+// rounding level of the quantities the Newton iteration produces
+constexpr double kRefineTol = 8.881784197001252e-16; // 2^-50
 
 __device__ __forceinline__ double ipowS(double x, int cnt)
 {
@@ -400,7 +403,7 @@ struct SparsePolicy
     }
 
     // mixed precision: FP32 factorisation of the row-scaled matrix, FP64 refinement
-    __device__ int mixedSolve(const SparseView& sp)
+    __device__ int mixedSolve(const SparseView& sp, double T)
     {
         for (int i = 0; i < D::n; ++i)
         {
@@ -442,7 +445,9 @@ struct SparsePolicy
             for (int i = 0; i < D::n; ++i)
             {
                 const double di = (double)d32[i], xi = x[i] + di;
-                conv &= fabs(di) <= kRefineTol * fabs(xi);
+                const int    o  = __ldg(sp.perm + i); // reference index: 0 = T, 1.. = species
+                const double sc = o == 0 ? T : fabs(Y[o - 1]);
+                conv &= fabs(di) <= kRefineTol * (fabs(xi) + sc);
                 x[i] = xi;
             }
             if (conv) return steps;
@@ -467,7 +472,7 @@ struct SparsePolicy
         assemble(nv, T, Tg, rho, drho_dt, cv, dpdT, dt);
         if constexpr (MIXED)
         {
-            const int steps = mixedSolve(nv.sp);
+            const int steps = mixedSolve(nv.sp, T);
             if (steps < 0)
             {
                 factorSolve64(nv.sp); // not converged: this system is solved in FP64

@@ -53,8 +53,8 @@ struct Request
     int                 ws = -1;
     cudaStream_t        stream = nullptr;
     cudaEvent_t         ev = nullptr;
-    unsigned long long* finished = nullptr; // host-mapped counter written by the kernel
-    unsigned long long* finishedDev = nullptr;
+    unsigned long long* finished    = nullptr; // pinned host copy of the counter below
+    unsigned long long* finishedDev = nullptr; // device counter of finished particles
     Clock::time_point   tSubmit, tDone;
     int                 slices = 0;
     std::string         error;
@@ -64,7 +64,7 @@ size_t requestBytes(int N, size_t P)
 {
     // Y, T, rho, dt, elapsed, nextT, drho, nit, cdDt, cdNt (8 B) + status, phase, nsub,
     // cdPower, cdSteps (4 B)
-    return P * ((size_t)(N + 10) * 8 + 5 * 4) + 4096;
+    return P * ((size_t)(N + 10) * 8 + 5 * 4) + 8192;
 }
 } // namespace
 
@@ -88,6 +88,7 @@ struct nnet_server_s
     Clock::time_point              tFirst, tLast;
     bool                           anyDone = false;
     unsigned long long             slices = 0;
+    unsigned long long*            pinned = nullptr; // completion-counter copies, one per workspace
 
     int  admit(Request* q);
     void launchSlice(Request* q);
@@ -102,9 +103,8 @@ int nnet_server_s::admit(Request* q)
     if (cudaStreamCreateWithFlags(&q->stream, cudaStreamNonBlocking) != cudaSuccess) return -1;
     if (cudaEventCreateWithFlags(&q->ev, cudaEventDisableTiming) != cudaSuccess) return -1;
     if (cudaMallocAsync((void**)&q->mem, q->bytes, q->stream) != cudaSuccess) return -1;
-    if (cudaHostAlloc((void**)&q->finished, sizeof(unsigned long long), cudaHostAllocMapped) != cudaSuccess) return -1;
+    q->finished  = pinned + q->ws; // one pinned slot per workspace (no allocation per request)
     *q->finished = 0;
-    cudaHostGetDevicePointer((void**)&q->finishedDev, q->finished, 0);
     const size_t P = q->P;
     char*        m = q->mem;
     auto         take = [&](size_t bytes) {
@@ -127,6 +127,8 @@ int nnet_server_s::admit(Request* q)
     q->rs.nsub    = (int*)take(4 * P);
     q->rs.cdPower = (int*)take(4 * P);
     q->rs.cdSteps = (int*)take(4 * P);
+    q->finishedDev = (unsigned long long*)take(sizeof(unsigned long long));
+    cudaMemsetAsync(q->finishedDev, 0, sizeof(unsigned long long), q->stream);
     cudaMemcpyAsync(q->Y, q->r.Y, sizeof(double) * P * q->N, cudaMemcpyHostToDevice, q->stream);
     cudaMemcpyAsync(q->T, q->r.T, sizeof(double) * P, cudaMemcpyHostToDevice, q->stream);
     cudaMemcpyAsync(q->rho, q->r.rho, sizeof(double) * P, cudaMemcpyHostToDevice, q->stream);
@@ -151,6 +153,7 @@ void nnet_server_s::launchSlice(Request* q)
         q->error = nnet_last_error_message();
         return;
     }
+    cudaMemcpyAsync(q->finished, q->finishedDev, sizeof(unsigned long long), cudaMemcpyDeviceToHost, q->stream);
     cudaEventRecord(q->ev, q->stream);
     ++q->slices, ++slices;
     q->state = Request::RUNNING;
@@ -236,7 +239,6 @@ void nnet_server_s::loop()
             {
                 cudaFreeAsync(q->mem, q->stream);
                 cudaStreamSynchronize(q->stream);
-                cudaFreeHost(q->finished);
                 cudaEventDestroy(q->ev);
                 cudaStreamDestroy(q->stream);
                 q->mem = nullptr, q->finished = nullptr;
@@ -279,12 +281,18 @@ int nnet_server_create(nnet_handle h, const nnet_server_config* cfg, nnet_server
     s->ws.resize(cfg->max_concurrent_requests);
     s->wsBusy.assign(cfg->max_concurrent_requests, 0);
     cudaSetDevice(h->device);
+    if (cudaMallocHost((void**)&s->pinned, sizeof(unsigned long long) * cfg->max_concurrent_requests) != cudaSuccess)
+    {
+        delete s;
+        return NNET_ERR_CUDA;
+    }
     const size_t scratch = maxScratchDoubles(h, cfg->solver);
     for (auto& w : s->ws)
         if (w.ensure(scratch, nullptr) != NNET_SUCCESS)
         {
             for (auto& x : s->ws)
                 x.release();
+            cudaFreeHost(s->pinned);
             delete s;
             return NNET_ERR_CUDA;
         }
@@ -368,6 +376,7 @@ int nnet_server_destroy(nnet_server s)
     cudaSetDevice(s->h->device);
     for (auto& w : s->ws)
         w.release();
+    cudaFreeHost(s->pinned);
     for (auto& kv : s->all)
         delete kv.second;
     delete s;

@@ -75,7 +75,12 @@ def _degenerate(den):
 
 
 def tables():
-    d, t = _grid()
+    return evaluate(*_grid())
+
+
+def evaluate(d, t):
+    """All 21 quantities of the model at density d (= rho Ye) and temperature t."""
+    d, t = np.asarray(d, dtype=np.float64), np.asarray(t, dtype=np.float64)
     nak = AVO * KERG
     lam3 = (H * H / (2.0 * np.pi * ME * KERG * t)) ** 1.5
     lnpsi = np.log(AVO * d * lam3 / 2.0)

@@ -178,3 +178,25 @@ def test_mixed_network_single_launch(ctx, solver):
         g = gpu_burn(ctx, w, solver)
         assert np.array_equal(b["Y"].cpu().numpy(), g[0]) and np.array_equal(b["T"].cpu().numpy(), g[1])
         assert np.array_equal(b["status"].cpu().numpy(), g[3])
+
+
+def test_text_table_loader_matches_binary(ctx, tmp_path):
+    """The reference-format text table (helmholtz.cpp:100-137) loads to the same EOS."""
+    import torch
+    import gen_helm_table
+    import nnet_gb300 as nn
+    path = gen_helm_table.write_reference_text(str(tmp_path / "helm_table.dat"))
+    c2 = nn.Context(0, helmholtz_table=path)
+    w = workloads.make("c2", P=256, seed=6)
+    Z = nn.network_charges(86)
+    dev = torch.device("cuda:0")
+    Y = torch.tensor(w["Y"], device=dev)
+    T, rho = torch.tensor(w["T"], device=dev), torch.tensor(w["rho"], device=dev)
+    a = [torch.zeros(256, dtype=torch.float64, device=dev) for _ in range(5)]
+    b = [torch.zeros(256, dtype=torch.float64, device=dev) for _ in range(5)]
+    ctx.helmholtz_eos(Z, T, rho, Y, *a)
+    c2.helmholtz_eos(Z, T, rho, Y, *b)
+    torch.cuda.synchronize()
+    for x, y in zip(a, b):
+        assert torch.equal(x, y)
+    c2.close()

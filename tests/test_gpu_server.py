@@ -20,7 +20,8 @@ def ctx():
 
 
 def request_arrays(w):
-    return (np.ascontiguousarray(w["Y"]), w["T"].copy(), w["rho"].copy(), w["dt"].copy(),
+    # fresh copies: the server writes results into the request's host buffers
+    return (np.array(w["Y"], order="C", copy=True), w["T"].copy(), w["rho"].copy(), w["dt"].copy(),
             np.zeros(w["T"].size, np.int32))
 
 

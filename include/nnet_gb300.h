@@ -78,6 +78,15 @@ enum nnet_solver
     NNET_SOLVER_MIXED       = 2, /* sparse LU factored in FP32, FP64 residual, iterative refinement */
 };
 
+/* How the sparse and mixed solvers map particles onto the GPU (no reference counterpart;
+ * the dense solver always runs one thread per particle, like the reference's kernel). */
+enum nnet_layout
+{
+    NNET_LAYOUT_AUTO   = 0, /* library choice (currently: warp per particle) */
+    NNET_LAYOUT_THREAD = 1, /* one thread per particle, Newton system in strided global scratch */
+    NNET_LAYOUT_WARP   = 2, /* one warp per particle, Newton system in shared memory */
+};
+
 typedef struct nnet_context* nnet_handle;
 
 /* Burn statistics accumulated over one nnet_burn call (device-side counters). */
@@ -206,6 +215,10 @@ int nnet_solver_info(int network, int solver, long long* factor_fma, long long* 
 /* Measured FP64 fused-multiply-add throughput of `device` in TFLOP/s (2 flops per FMA)
  * with a dependency-free probe kernel (no reference counterpart; roofline denominator). */
 int nnet_measure_fp64_peak(int device, double* tflops);
+
+/* Select the particle layout of the sparse and mixed solvers for later nnet_burn calls on
+ * `h` (nnet_layout; no reference counterpart: chosen by the autotuner). */
+int nnet_set_layout(nnet_handle h, int layout);
 
 /* Number of species / reactions of a network, 0 on success. */
 int nnet_network_info(int network, int* num_species, int* num_reactions);

@@ -111,6 +111,15 @@ int uploadNetwork(int net, NetBuffer& b)
                  oUCol = putv(sp.uCol), oTPos = putv(sp.tPos), oDiag = putv(sp.diagPos), oCol0 = putv(sp.col0Pos),
                  oRow0 = putv(sp.row0Pos), oCBeg = putv(sp.cBeg), oCPos = putv(sp.cPos), oCRow = putv(sp.cRow),
                  oSb = putv(sp.sbPos), oSbD = putv(sp.sbDiag);
+    // warp-per-particle lists
+    const WarpPlan wp = buildWarpPlan(sp, rbeg, rspec, rcnt, pbeg, pspec, pcnt);
+    const size_t oSgC = putd(wp.sgCoef.data(), wp.sgCoef.size()), oJgC = putd(wp.jgCoef.data(), wp.jgCoef.size());
+    const size_t oUpdB = putv(wp.updBeg), oUpdT = putv(wp.updT), oUpdL = putv(wp.updL), oUpdU = putv(wp.updU),
+                 oUcB = putv(wp.ucBeg), oUcP = putv(wp.ucPos), oUcR = putv(wp.ucRow), oSgB = putv(wp.sgBeg),
+                 oSgR = putv(wp.sgRx), oJP = putv(wp.jPos), oJR = putv(wp.jRow), oJC = putv(wp.jCol),
+                 oJgB = putv(wp.jgBeg), oJgE = putv(wp.jgEnt), oRjB = putv(wp.rjBeg), oRjE = putv(wp.rjEnt),
+                 oERx = putv(wp.entRx), oSgH = putv(wp.sgHeavy), oJgH = putv(wp.jgHeavy), oRjH = putv(wp.rjHeavy),
+                 oRowH = putv(wp.rowHeavy);
     const size_t bytesD = d.size() * sizeof(double), bytes = bytesD + ii.size() * sizeof(int);
     NNET_CUDA(cudaMalloc(&b.mem, bytes));
     NNET_CUDA(cudaMemcpy(b.mem, d.data(), bytesD, cudaMemcpyHostToDevice));
@@ -131,6 +140,14 @@ int uploadNetwork(int net, NetBuffer& b)
     w.uBeg = I + oUBeg, w.uPos = I + oUPos, w.uCol = I + oUCol, w.tPos = I + oTPos;
     w.diagPos = I + oDiag, w.col0Pos = I + oCol0, w.row0Pos = I + oRow0, w.cBeg = I + oCBeg, w.cPos = I + oCPos;
     w.cRow = I + oCRow, w.sbPos = I + oSb, w.sbDiag = I + oSbD, w.cCoef = D + oCoef;
+    WarpView& x = v.wv;
+    x.nJ = (int)wp.jPos.size(), x.nEnt = (int)wp.entRx.size(), x.nSgHeavy = (int)wp.sgHeavy.size();
+    x.nJgHeavy = (int)wp.jgHeavy.size(), x.nRjHeavy = (int)wp.rjHeavy.size(), x.nRowHeavy = (int)wp.rowHeavy.size();
+    x.updBeg = I + oUpdB, x.updT = I + oUpdT, x.updL = I + oUpdL, x.updU = I + oUpdU, x.ucBeg = I + oUcB;
+    x.ucPos = I + oUcP, x.ucRow = I + oUcR, x.sgBeg = I + oSgB, x.sgRx = I + oSgR, x.jPos = I + oJP, x.jRow = I + oJR;
+    x.jCol = I + oJC, x.jgBeg = I + oJgB, x.jgEnt = I + oJgE, x.rjBeg = I + oRjB, x.rjEnt = I + oRjE;
+    x.entRx = I + oERx, x.sgHeavy = I + oSgH, x.jgHeavy = I + oJgH, x.rjHeavy = I + oRjH, x.rowHeavy = I + oRowH;
+    x.sgCoef = D + oSgC, x.jgCoef = D + oJgC;
     return NNET_SUCCESS;
 }
 
@@ -373,14 +390,21 @@ void nnet_gb300::Workspace::release()
     scratch = nullptr, counters = nullptr, doubles = 0;
 }
 
+KernelInfo nnet_gb300::burnKernel(nnet_context* h, int net, int eos, int solver)
+{
+    if (solver == NNET_SOLVER_DENSE_FP64) return denseKernel(net, eos);
+    const int mixed = solver == NNET_SOLVER_MIXED;
+    return h->layout == NNET_LAYOUT_THREAD ? sparseKernel(net, eos, mixed) : warpKernel(net, eos, mixed);
+}
+
 size_t nnet_gb300::maxScratchDoubles(nnet_context* h, int solver)
 {
     size_t m = 0;
     for (int net : {14, 86, 87})
         for (int eos : {0, 1})
         {
-            KernelInfo ki = solver == NNET_SOLVER_DENSE_FP64 ? denseKernel(net, eos)
-                                                             : sparseKernel(net, eos, solver == NNET_SOLVER_MIXED);
+            const KernelInfo ki = burnKernel(h, net, eos, solver);
+            if (!ki.perSlot) continue;
             int perSM = 0;
             if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, ki.func, ki.block, 0) != cudaSuccess) perSM = 1;
             m = std::max(m, (size_t)h->numSMs * std::max(perSM, 1) * ki.block * ki.perSlot);
@@ -426,10 +450,13 @@ void fillParams(const nnet_burn_args* a, unsigned long long* counters, BurnParam
 int gridFor(nnet_context* h, const KernelInfo& ki, size_t P, size_t& blocks, size_t& slots)
 {
     int perSM = 0;
-    NNET_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, ki.func, ki.block, 0));
-    if (perSM < 1) perSM = 1;
+    if (ki.smem > 48 * 1024)
+        NNET_CUDA(cudaFuncSetAttribute(ki.func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ki.smem));
+    NNET_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, ki.func, ki.block, ki.smem));
+    if (perSM < 1) return fail(NNET_ERR_TOO_LARGE, "burn kernel does not fit on an SM");
     const size_t maxBlocks = (size_t)h->numSMs * perSM;
-    const size_t need      = (P + ki.block - 1) / ki.block;
+    const size_t perBlock  = ki.smem ? ki.block / 32 : ki.block; // particles in flight per block
+    const size_t need      = (P + perBlock - 1) / perBlock;
     blocks                 = need < maxBlocks ? need : maxBlocks;
     slots                  = blocks * ki.block;
     return NNET_SUCCESS;
@@ -443,8 +470,7 @@ int nnet_gb300::launchBurn(nnet_context* h, const nnet_burn_args* a, Workspace& 
     if (a->num_particles == 0) return NNET_SUCCESS;
     NNET_CUDA(cudaSetDevice(h->device));
     const int  ni = netIndex(a->network);
-    KernelInfo ki = a->solver == NNET_SOLVER_DENSE_FP64 ? denseKernel(a->network, a->eos)
-                                                        : sparseKernel(a->network, a->eos, a->solver == NNET_SOLVER_MIXED);
+    const KernelInfo ki = burnKernel(h, a->network, a->eos, a->solver);
     if (ki.maxNnz && h->nets[ni].plan.nnz > ki.maxNnz)
         return fail(NNET_ERR_TOO_LARGE, "sparse factor does not fit the kernel's storage");
     size_t blocks, slots;
@@ -462,7 +488,15 @@ int nnet_gb300::launchBurn(nnet_context* h, const nnet_burn_args* a, Workspace& 
     double*  sc     = ws.scratch;
     size_t   stride = slots;
     void*    args[] = {&bp, &nv, &hv, &sc, &stride};
-    NNET_CUDA(cudaLaunchKernel(ki.func, dim3((unsigned)blocks), dim3(ki.block), args, 0, st));
+    NNET_CUDA(cudaLaunchKernel(ki.func, dim3((unsigned)blocks), dim3(ki.block), args, ki.smem, st));
+    return NNET_SUCCESS;
+}
+
+extern "C" int nnet_set_layout(nnet_handle h, int layout)
+{
+    if (!h) return fail(NNET_ERR_INVALID, "null handle");
+    if (layout < NNET_LAYOUT_AUTO || layout > NNET_LAYOUT_WARP) return fail(NNET_ERR_INVALID, "unknown layout");
+    h->layout = layout;
     return NNET_SUCCESS;
 }
 

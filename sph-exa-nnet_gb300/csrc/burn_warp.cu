@@ -1,0 +1,747 @@
+// Warp-per-particle forms of the sparse and mixed-precision burn.
+//
+// The thread-per-particle kernels keep each particle's Newton system in per-slot global
+// scratch (about 25 KB per net86 particle), so every update of the matrix is a dependent
+// round trip to L2/HBM and the kernel is latency-bound.  Here one warp owns one particle at
+// a time and the whole system lives in shared memory (about 23 KB per warp for net86):
+//   * species-, reaction- and matrix-entry-parallel phases are spread over the 32 lanes;
+//   * accumulations are gathers in a fixed order (WarpPlan), and the few long lists (the
+//     p, n, alpha rows and columns) are split across the warp and summed with a fixed
+//     butterfly, so no two lanes write one word and results are deterministic;
+//   * the right-looking LU runs pivot by pivot: multipliers, then the pivot's independent
+//     updates in parallel; forward substitution by columns of L, backward by columns of U;
+//   * scalar work (EOS, special rates, Newton control) is evaluated identically by every
+//     lane, so control flow is warp-uniform.
+// The mixed form factors in FP32 (cheap reciprocals, FP32 pipe) with FP64 residuals; the
+// FP64 pipe, which bounds GB300 here, then only sees rates, assembly and residuals.
+#include "burn_policies.cuh"
+#include "launch.hpp"
+#include "sparse_plan.hpp"
+
+namespace nnet_gb300
+{
+
+constexpr unsigned kFull = 0xffffffffu;
+
+__device__ __forceinline__ double warpSum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_xor_sync(kFull, v, o);
+    return v;
+}
+
+template<int NET>
+struct WDims
+{
+    static constexpr int N   = NET, n = NET + 1;
+    static constexpr int R   = NetDims<NET>::R;
+    static constexpr int NE  = NET == 14 ? 42 : NET == 86 ? 482 : 486; // reactant entries
+    static constexpr int NNZ = NET == 14 ? 104 : 1056;                 // factor capacity (checked on host)
+};
+
+// shared-memory layout of one warp (doubles; the float factor of the mixed form overlaps
+// the Jacobian bases `tr`, which are consumed before the solve)
+template<int NET, bool MIXED>
+struct WarpSmem
+{
+    using D = WDims<NET>;
+    static constexpr int oY = 0, oYn = oY + D::N, oF = oYn + D::N, oDF = oF + D::R, oBE = oDF + D::R,
+                         oA = oBE + D::N, oB = oA + D::NNZ, oDYdt = oB + D::n, oDYdT = oDYdt + D::N,
+                         oJdy = oDYdT + D::N, oTr = oJdy + D::N;
+    static constexpr int floatsD = (D::NNZ + D::n + 1) / 2;
+    static constexpr int doubles = oTr + (MIXED && floatsD > D::NE ? floatsD : D::NE);
+
+    static_assert(4 * D::n <= 2 * D::R + D::N, "solve vectors must fit the flux storage");
+    double *Y, *Yn, *f, *df, *BE, *A, *b, *dYdt, *mu, *dYdT, *jdy, *tr, *x, *r, *ipiv, *scale;
+    float * LU, *d;
+
+    __device__ explicit WarpSmem(double* s)
+    {
+        Y = s + oY, Yn = s + oYn, f = s + oF, df = s + oDF, BE = s + oBE, A = s + oA, b = s + oB;
+        dYdt = s + oDYdt, dYdT = s + oDYdT, jdy = s + oJdy, tr = s + oTr;
+        mu = dYdt; // screening potentials live until the rates are done
+        // the solve vectors reuse the flux / binding-energy storage, dead after assembly
+        x = f, r = f + D::n, ipiv = f + 2 * D::n, scale = f + 3 * D::n;
+        LU = reinterpret_cast<float*>(tr), d = LU + D::NNZ;
+    }
+};
+
+// ------------------------------------------------------------------ rates (warp)
+template<int NET, bool MIXED>
+__device__ void warpRates(const NetView& nv, WarpSmem<NET, MIXED>& S, double T, double rho, int lane)
+{
+    const CoulombFast cf(T, rho);
+    constexpr int     NS = NET == 14 ? 14 : 86;
+    for (int i = lane; i < NS; i += 32)
+    {
+        S.BE[i] = cf.be(nv, i);
+        S.mu[i] = (NET != 14 && i == 1) ? 0. : cf.mu(nv, i); // neutrons carry no screening
+    }
+    __syncwarp();
+    const FitT   v(T);
+    const double twoT = 2. / T;
+    const int    kb   = temperatureRange(T);
+    Special      s;
+    if constexpr (NET == 14)
+    {
+        const double t9 = T / 1.e9, t9i = 1.e0 / t9, lt9 = log(t9);
+        const double val1 = 11.6045e0 * t9i, val2 = 1.5e0 * lt9, val3 = val1 * t9i * 1e-9, val4 = 1.5e-9 * t9i;
+        for (int i = 4 + lane; i < 14; i += 32)
+        {
+            const double* f  = nv.fit + (i - 4) * 8;
+            const double  f0 = __ldg(f), f1 = __ldg(f + 1), f2 = __ldg(f + 2), f3 = __ldg(f + 3),
+                         f4 = __ldg(f + 4), f5 = __ldg(f + 5), f6 = __ldg(f + 6), f7 = __ldg(f + 7);
+            const double coef  = f1 * v.t9i + f2 * v.t9i13 + f3 * v.t913 + f4 * v.t9 + f5 * v.t953 + f6 * v.lt9;
+            const double dcoef = (-f1 * v.t9i2 + (-f2 * v.t9i43 + f3 * v.t9i23 + 5 * f5 * v.t923) * (1. / 3.) + f4 +
+                                  f6 * v.t9i) *
+                                 1e-9;
+            const double q   = __ldg(nv.q + i - 4);
+            const double dmu = S.mu[i - 1] + S.mu[0] - S.mu[i];
+            const double e = exp(f0 + coef + dmu), de = e * (dcoef - dmu * twoT);
+            const double l = __ldg(nv.choose + (i - 4) * 24 + kb) / __ldg(nv.choose + (i + 1 - 4) * 24 + kb) *
+                             exp(coef + f7 - q * val1 + val2);
+            S.f[i - 1] = e, S.df[i - 1] = de;
+            S.f[16 + i - 1] = l, S.df[16 + i - 1] = l * (dcoef + q * val3 + val4);
+        }
+        specialRates(T, s);
+        const double* m = S.mu;
+        screenFast(s.e3a, s.de3a, m[0] + m[0] - m[1] + m[0], T);
+        screenFast(s.ecag, s.decag, m[1] + m[0] - m[2], T);
+        screenFast(s.eoag, s.deoag, m[2] + m[0] - m[3], T);
+        screenFast(s.e2c, s.de2c, 2. * m[1] - m[3], T);
+        screenFast(s.eco, s.deco, m[1] + m[2] - m[4], T);
+        screenFast(s.e2o, s.de2o, 2. * m[2] - m[5], T);
+        if (lane == 0)
+        {
+            S.f[0] = s.e3a, S.df[0] = s.de3a, S.f[1] = s.ecag, S.df[1] = s.decag;
+            S.f[2] = s.eoag, S.df[2] = s.deoag, S.f[13] = s.e2c, S.df[13] = s.de2c;
+            S.f[14] = s.eco, S.df[14] = s.deco, S.f[15] = s.e2o, S.df[15] = s.de2o;
+            S.f[16] = s.l3a, S.df[16] = s.dl3a, S.f[17] = s.lcag, S.df[17] = s.dlcag;
+            S.f[18] = s.loag, S.df[18] = s.dloag;
+        }
+    }
+    else
+    {
+        const double t9 = T * 1e-09, t9i = 1. / t9;
+        const double val1 = 11.6045 * t9i, val2 = 1.5 * log(t9), val3 = val1 * t9i * 1e-9, val4 = 1.5e-9 * t9i;
+        for (int i = 7 + lane; i < 157; i += 32)
+        {
+            const double* f  = nv.fit + (i - 7) * 8;
+            const double  f0 = __ldg(f), f1 = __ldg(f + 1), f2 = __ldg(f + 2), f3 = __ldg(f + 3),
+                         f4 = __ldg(f + 4), f5 = __ldg(f + 5), f6 = __ldg(f + 6), f7 = __ldg(f + 7);
+            const double coef  = f1 * v.t9i + f2 * v.t9i13 + f3 * v.t913 + f4 * v.t9 + f5 * v.t953 + f6 * v.lt9;
+            const double dcoef = (-f1 * v.t9i2 + (-f2 * v.t9i43 + f3 * v.t9i23 + 5 * f5 * v.t923) * (1. / 3.) + f4 +
+                                  f6 * v.t9i) *
+                                 1e-9;
+            const int    mr = __ldg(nv.mainReactant + i), sr = __ldg(nv.secondaryReactant + i),
+                      mp = __ldg(nv.mainProduct + i);
+            const double part = __ldg(nv.choose + (mr - 5) * 24 + kb) / __ldg(nv.choose + (mp - 5) * 24 + kb);
+            const double q    = __ldg(nv.q + i - 7);
+            const double dmu  = S.mu[mr] + S.mu[sr] - S.mu[mp];
+            const double sdmu = i >= 137 ? dmu : 0.;
+            const double xr   = f7 + coef - val1 * q + (i < 137 ? val2 : 0.);
+            const double dr   = dcoef + val3 * q + (i < 137 ? val4 : 0.);
+            double       e, de, l, dl;
+            if ((i >= 137 && i < 154) || i == 156)
+            {
+                e = part * exp(xr + dmu), de = e * (dr - dmu * twoT);
+                l = exp(f0 + coef + sdmu), dl = l * (dcoef - sdmu * twoT);
+            }
+            else
+            {
+                e = exp(f0 + coef + dmu), de = e * (dcoef - dmu * twoT);
+                l = part * exp(xr + sdmu), dl = l * (dr - sdmu * twoT);
+            }
+            S.f[fwdSlot86(i)] = e, S.df[fwdSlot86(i)] = de;
+            S.f[revSlot86(i)] = l, S.df[revSlot86(i)] = dl;
+        }
+        specialRates(T, s);
+        auto dmu = [&](int i) {
+            return S.mu[__ldg(nv.mainReactant + i)] + S.mu[__ldg(nv.secondaryReactant + i)] -
+                   S.mu[__ldg(nv.mainProduct + i)];
+        };
+        screenFast(s.e2c, s.de2c, dmu(0), T);
+        screenFast(s.eco, s.deco, dmu(1), T);
+        screenFast(s.e2o, s.de2o, dmu(2), T);
+        screenFast(s.e3a, s.de3a, dmu(4) + S.mu[__ldg(nv.mainReactant + 4)], T);
+        screenFast(s.ecag, s.decag, dmu(5), T);
+        screenFast(s.eoag, s.deoag, dmu(6), T);
+        if (lane == 0)
+        {
+            S.f[0] = s.e2c, S.df[0] = s.de2c, S.f[1] = s.eco, S.df[1] = s.deco;
+            S.f[2] = s.e2o, S.df[2] = s.de2o, S.f[3] = s.e3a, S.df[3] = s.de3a;
+            S.f[4] = s.ecag, S.df[4] = s.decag, S.f[5] = s.eoag, S.df[5] = s.deoag;
+            S.f[revSlot86(4)] = s.l3a, S.df[revSlot86(4)] = s.dl3a;
+            S.f[revSlot86(5)] = s.lcag, S.df[revSlot86(5)] = s.dlcag;
+            S.f[revSlot86(6)] = s.loag, S.df[revSlot86(6)] = s.dloag;
+        }
+        if constexpr (NET == 87)
+        {
+            // electron captures (net87.hpp:117-175)
+            const double rhoElec = S.Yn[86] * rho;
+            double       ev[12];
+            electronRates(nv, T, rhoElec, ev);
+            const double kbt = NNET_KB * T, nakbt = NNET_NA * kbt;
+            if (lane == 0)
+            {
+                S.BE[86] = __ldg(nv.BE + 86) + -1.5 * nakbt;
+                S.BE[0]  = S.BE[0] + -ev[3];
+                S.BE[1]  = S.BE[1] + -ev[9];
+                S.f[309] = rhoElec == 0 ? 0 : ev[0] / rhoElec, S.df[309] = rhoElec == 0 ? 0 : ev[1] / rhoElec;
+                S.f[310] = rhoElec == 0 ? 0 : ev[6] / rhoElec, S.df[310] = rhoElec == 0 ? 0 : ev[7] / rhoElec;
+            }
+        }
+    }
+    __syncwarp();
+}
+
+// ------------------------------------------------------------------ assembly (warp)
+template<int NET, bool MIXED>
+__device__ void warpAssemble(const NetView& nv, WarpSmem<NET, MIXED>& S, double T, double Tg, double rho,
+                             double drho_dt, double cv, double dpdT, double dt, int lane)
+{
+    using D                = WDims<NET>;
+    const SparseView& sp   = nv.sp;
+    const WarpView&   wv   = nv.wv;
+    // per-reaction fluxes (dY/dt terms, nuclear_net.hpp:347-381) and Jacobian bases
+    // (:395-438), in place of the rates
+    for (int q = lane; q < D::R; q += 32)
+    {
+        const int rb = __ldg(nv.rbeg + q), re = __ldg(nv.rbeg + q + 1);
+        double    f = S.f[q], df = S.df[q], base = f;
+        for (int k = rb; k < re; ++k)
+        {
+            const int    cnt = __ldg(nv.rcnt + k);
+            const double yr  = S.Yn[__ldg(nv.rspec + k)] * rho;
+            if (cnt != 1)
+            {
+                const double fac = cnt == 2 ? 2. : 6.;
+                f /= fac, df /= fac, base /= fac;
+            }
+            const double pw = ipowS(yr, cnt);
+            f *= pw, df *= pw, base *= ipowS(yr, cnt - 1);
+        }
+        S.f[q] = f / rho, S.df[q] = df / rho;
+        for (int k = rb; k < re; ++k)
+        {
+            const int id = __ldg(nv.rspec + k);
+            double    tr = base;
+            for (int o = rb; o < re; ++o)
+            {
+                const int os = __ldg(nv.rspec + o);
+                if (os != id) tr *= S.Yn[os] * rho;
+            }
+            S.tr[k] = base > k::epsilonSystem ? tr : 0.;
+        }
+    }
+    for (int p = lane; p < sp.nnz; p += 32)
+        S.A[p] = 0.;
+    __syncwarp();
+    // dY/dt and d(dY/dt)/dT per species
+    for (int s = lane; s < D::N; s += 32)
+    {
+        const int b0 = __ldg(wv.sgBeg + s), b1 = __ldg(wv.sgBeg + s + 1);
+        if (b1 - b0 > WarpPlan::kHeavy) continue;
+        double a = 0, c = 0;
+        for (int k = b0; k < b1; ++k)
+        {
+            const double w = __ldg(wv.sgCoef + k);
+            const int    r = __ldg(wv.sgRx + k);
+            a += w * S.f[r], c += w * S.df[r];
+        }
+        S.dYdt[s] = a, S.dYdT[s] = c;
+    }
+    for (int h = 0; h < wv.nSgHeavy; ++h)
+    {
+        const int s = __ldg(wv.sgHeavy + h), b0 = __ldg(wv.sgBeg + s), b1 = __ldg(wv.sgBeg + s + 1);
+        double    a = 0, c = 0;
+        for (int k = b0 + lane; k < b1; k += 32)
+        {
+            const double w = __ldg(wv.sgCoef + k);
+            const int    r = __ldg(wv.sgRx + k);
+            a += w * S.f[r], c += w * S.df[r];
+        }
+        a = warpSum(a), c = warpSum(c);
+        if (lane == 0) S.dYdt[s] = a, S.dYdT[s] = c;
+    }
+    // Jacobian entries
+    for (int m = lane; m < wv.nJ; m += 32)
+    {
+        const int b0 = __ldg(wv.jgBeg + m), b1 = __ldg(wv.jgBeg + m + 1);
+        if (b1 - b0 > WarpPlan::kHeavy) continue;
+        double a = 0;
+        for (int k = b0; k < b1; ++k)
+            a += __ldg(wv.jgCoef + k) * S.tr[__ldg(wv.jgEnt + k)];
+        S.A[__ldg(wv.jPos + m)] = a;
+    }
+    for (int h = 0; h < wv.nJgHeavy; ++h)
+    {
+        const int m = __ldg(wv.jgHeavy + h), b0 = __ldg(wv.jgBeg + m), b1 = __ldg(wv.jgBeg + m + 1);
+        double    a = 0;
+        for (int k = b0 + lane; k < b1; k += 32)
+            a += __ldg(wv.jgCoef + k) * S.tr[__ldg(wv.jgEnt + k)];
+        a = warpSum(a);
+        if (lane == 0) S.A[__ldg(wv.jPos + m)] = a;
+    }
+    __syncwarp();
+    // J (Yg - Y) per species row (nuclear_net.hpp:580-589)
+    for (int i = lane; i < D::N; i += 32)
+    {
+        const int b0 = __ldg(wv.rjBeg + i), b1 = __ldg(wv.rjBeg + i + 1);
+        if (b1 - b0 > WarpPlan::kHeavy) continue;
+        double a = 0;
+        for (int k = b0; k < b1; ++k)
+        {
+            const int m = __ldg(wv.rjEnt + k), j = __ldg(wv.jCol + m);
+            a += S.A[__ldg(wv.jPos + m)] * (S.Yn[j] - S.Y[j]);
+        }
+        S.jdy[i] = a;
+    }
+    for (int h = 0; h < wv.nRjHeavy; ++h)
+    {
+        const int i = __ldg(wv.rjHeavy + h), b0 = __ldg(wv.rjBeg + i), b1 = __ldg(wv.rjBeg + i + 1);
+        double    a = 0;
+        for (int k = b0 + lane; k < b1; k += 32)
+        {
+            const int m = __ldg(wv.rjEnt + k), j = __ldg(wv.jCol + m);
+            a += S.A[__ldg(wv.jPos + m)] * (S.Yn[j] - S.Y[j]);
+        }
+        a = warpSum(a);
+        if (lane == 0) S.jdy[i] = a;
+    }
+    __syncwarp();
+    // I - theta dt J, the temperature row / column and the right-hand side (:590-608)
+    const double mtd = -k::theta * dt;
+    for (int e = lane; e < sp.nsb; e += 32)
+    {
+        const int p = __ldg(sp.sbPos + e);
+        S.A[p]      = __ldg(sp.sbDiag + e) ? 1. - k::theta * dt * S.A[p] : mtd * S.A[p];
+    }
+    for (int i = lane; i < D::N; i += 32)
+    {
+        const double c0 = S.dYdT[i];
+        double       rh = S.dYdt[i] * dt;
+        rh              = rh + mtd * c0 * (Tg - T);
+        rh              = rh + mtd * S.jdy[i];
+        S.b[__ldg(sp.iperm + i + 1)] = rh;
+        S.A[__ldg(sp.col0Pos + i)]   = c0 * mtd;
+        S.A[__ldg(sp.row0Pos + i)]   = -S.BE[i] / cv;
+    }
+    if (lane == 0)
+    {
+        const double drho = drho_dt * dt, value1 = dpdT * drho / (rho * rho);
+        S.b[sp.tNew]  = T * value1 / cv;
+        S.A[sp.pos00] = 1 - k::theta * value1 / cv;
+    }
+    __syncwarp();
+}
+
+// ------------------------------------------------------------------ solves (warp)
+// FP64: factor A in place, x = A^-1 b (x aliases nothing the factor uses)
+template<int NET, bool MIXED>
+__device__ void warpSolve64(const NetView& nv, WarpSmem<NET, MIXED>& S, int lane)
+{
+    using D              = WDims<NET>;
+    const SparseView& sp = nv.sp;
+    const WarpView&   wv = nv.wv;
+    for (int k = 0; k < D::n; ++k)
+    {
+        const double ip = __drcp_rn(S.A[__ldg(sp.kPiv + k)]);
+        for (int e = __ldg(sp.lBeg + k) + lane; e < __ldg(sp.lBeg + k + 1); e += 32)
+            S.A[__ldg(sp.lPos + e)] *= ip;
+        if (lane == 0) S.ipiv[k] = ip;
+        __syncwarp();
+        for (int q = __ldg(wv.updBeg + k) + lane; q < __ldg(wv.updBeg + k + 1); q += 32)
+        {
+            const int t = __ldg(wv.updT + q);
+            S.A[t]      = S.A[t] - S.A[__ldg(wv.updL + q)] * S.A[__ldg(wv.updU + q)];
+        }
+        __syncwarp();
+    }
+    for (int i = lane; i < D::n; i += 32)
+        S.x[i] = S.b[i];
+    __syncwarp();
+    for (int k = 0; k < D::n; ++k)
+    {
+        const double bk = S.x[k];
+        for (int e = __ldg(sp.lBeg + k) + lane; e < __ldg(sp.lBeg + k + 1); e += 32)
+        {
+            const int i = __ldg(sp.lRow + e);
+            S.x[i]      = S.x[i] - S.A[__ldg(sp.lPos + e)] * bk;
+        }
+        __syncwarp();
+    }
+    for (int k = D::n - 1; k >= 0; --k)
+    {
+        const double xk = S.x[k] * S.ipiv[k];
+        __syncwarp();
+        if (lane == 0) S.x[k] = xk;
+        for (int q = __ldg(wv.ucBeg + k) + lane; q < __ldg(wv.ucBeg + k + 1); q += 32)
+        {
+            const int i = __ldg(wv.ucRow + q);
+            S.x[i]      = S.x[i] - S.A[__ldg(wv.ucPos + q)] * xk;
+        }
+        __syncwarp();
+    }
+}
+
+// FP32 triangular solves on S.d (in place)
+template<int NET>
+__device__ void warpSolve32(const NetView& nv, WarpSmem<NET, true>& S, int lane)
+{
+    using D              = WDims<NET>;
+    const SparseView& sp = nv.sp;
+    const WarpView&   wv = nv.wv;
+    for (int k = 0; k < D::n; ++k)
+    {
+        const float bk = S.d[k];
+        for (int e = __ldg(sp.lBeg + k) + lane; e < __ldg(sp.lBeg + k + 1); e += 32)
+        {
+            const int i = __ldg(sp.lRow + e);
+            S.d[i]      = S.d[i] - S.LU[__ldg(sp.lPos + e)] * bk;
+        }
+        __syncwarp();
+    }
+    for (int k = D::n - 1; k >= 0; --k)
+    {
+        const float xk = S.d[k] * (float)S.ipiv[k];
+        __syncwarp();
+        if (lane == 0) S.d[k] = xk;
+        for (int q = __ldg(wv.ucBeg + k) + lane; q < __ldg(wv.ucBeg + k + 1); q += 32)
+        {
+            const int i = __ldg(wv.ucRow + q);
+            S.d[i]      = S.d[i] - S.LU[__ldg(wv.ucPos + q)] * xk;
+        }
+        __syncwarp();
+    }
+}
+
+// rows scaled by powers of two, FP32 factorisation, FP64 residual refinement; returns
+// the refinement steps, or -1 if the corrections did not settle (caller re-solves in FP64)
+template<int NET>
+__device__ int warpSolveMixed(const NetView& nv, WarpSmem<NET, true>& S, double T, int lane, double* scale)
+{
+    using D              = WDims<NET>;
+    const SparseView& sp = nv.sp;
+    const WarpView&   wv = nv.wv;
+    // row scales from the exponent bits (integer work), then the FP32 copy
+    for (int i = lane; i < D::n; i += 32)
+    {
+        int e = 0;
+        for (int p = __ldg(sp.rowBeg + i), pe = __ldg(sp.rowBeg + i + 1); p < pe; ++p)
+            e = max(e, (int)((__double_as_longlong(S.A[p]) >> 52) & 0x7ff));
+        scale[i] = e == 0 ? 1. : ldexp(1., 1023 - e); // 2^-ilogb(max |a_ij|)
+    }
+    __syncwarp();
+    for (int p = lane; p < sp.nnz; p += 32)
+        S.LU[p] = (float)(S.A[p] * scale[__ldg(sp.posRow + p)]);
+    __syncwarp();
+    for (int k = 0; k < D::n; ++k)
+    {
+        const float ip = 1.f / S.LU[__ldg(sp.kPiv + k)];
+        for (int e = __ldg(sp.lBeg + k) + lane; e < __ldg(sp.lBeg + k + 1); e += 32)
+            S.LU[__ldg(sp.lPos + e)] *= ip;
+        if (lane == 0) S.ipiv[k] = ip;
+        __syncwarp();
+        for (int q = __ldg(wv.updBeg + k) + lane; q < __ldg(wv.updBeg + k + 1); q += 32)
+        {
+            const int t = __ldg(wv.updT + q);
+            S.LU[t]     = S.LU[t] - S.LU[__ldg(wv.updL + q)] * S.LU[__ldg(wv.updU + q)];
+        }
+        __syncwarp();
+    }
+    for (int i = lane; i < D::n; i += 32)
+        S.x[i] = 0., S.r[i] = S.b[i];
+    __syncwarp();
+    for (int steps = 0;; ++steps)
+    {
+        for (int i = lane; i < D::n; i += 32)
+            S.d[i] = (float)(S.r[i] * scale[i]);
+        __syncwarp();
+        warpSolve32<NET>(nv, S, lane);
+        bool conv = true;
+        for (int i = lane; i < D::n; i += 32)
+        {
+            const double di = (double)S.d[i], xi = S.x[i] + di;
+            const int    o  = __ldg(sp.perm + i);
+            const double sc = o == 0 ? T : fabs(S.Y[o - 1]);
+            conv &= fabs(di) <= kRefineTol * (fabs(xi) + sc);
+            S.x[i] = xi;
+        }
+        conv = __all_sync(kFull, conv);
+        __syncwarp();
+        if (conv) return steps;
+        if (steps == kMaxRefine) return -1;
+        // r = b - A x (FP64, rows over lanes; the long rows split across the warp)
+        for (int i = lane; i < D::n; i += 32)
+        {
+            const int p0 = __ldg(sp.rowBeg + i), p1 = __ldg(sp.rowBeg + i + 1);
+            if (p1 - p0 > WarpPlan::kHeavy) continue;
+            double s = S.b[i];
+            for (int p = p0; p < p1; ++p)
+                s -= S.A[p] * S.x[__ldg(sp.posCol + p)];
+            S.r[i] = s;
+        }
+        for (int h = 0; h < wv.nRowHeavy; ++h)
+        {
+            const int i = __ldg(wv.rowHeavy + h), p0 = __ldg(sp.rowBeg + i), p1 = __ldg(sp.rowBeg + i + 1);
+            double    s = 0;
+            for (int p = p0 + lane; p < p1; p += 32)
+                s += S.A[p] * S.x[__ldg(sp.posCol + p)];
+            s = warpSum(s);
+            if (lane == 0) S.r[i] = S.b[i] - s;
+        }
+        __syncwarp();
+    }
+}
+
+// ------------------------------------------------------------------ driver (warp)
+template<int NET, int EOS, bool MIXED>
+__global__ void __launch_bounds__(128) burnWarpKernel(BurnParams bp, NetView nv, HelmView hv, double* /*unused*/,
+                                                      size_t /*unused*/)
+{
+    using D = WDims<NET>;
+    extern __shared__ __align__(16) double smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double*   base = smem + (size_t)warp * WarpSmem<NET, MIXED>::doubles;
+    WarpSmem<NET, MIXED> S(base);
+    const SparseView& sp = nv.sp;
+
+    ParticleState s;
+    for (;;)
+    {
+        // ---- acquire (lane 0 takes the queue index; every lane then reads the same words)
+        unsigned long long q = 0;
+        if (lane == 0) q = atomicAdd(bp.queue, 1ull);
+        q = __shfl_sync(kFull, q, 0);
+        if (q >= bp.P) break;
+        const size_t p     = bp.order ? (size_t)bp.order[q] : (size_t)q;
+        const int    phase = bp.rs.phase ? bp.rs.phase[p] : 0;
+        if (phase == 2) continue;
+        const double rho0 = bp.rho[p], T0 = bp.T[p];
+        if (phase == 0 && !(rho0 > k::minRho && T0 > k::minTemp))
+        {
+            if (lane == 0)
+            {
+                if (bp.status) bp.status[p] = ST_SKIPPED;
+                if (bp.substeps) bp.substeps[p] = 0;
+                if (bp.iterations) bp.iterations[p] = 0;
+                atomicAdd(bp.stats + 2 + ST_SKIPPED, 1ull);
+                finishSegment(bp, p);
+            }
+            continue;
+        }
+        for (int j = lane; j < D::N; j += 32)
+            S.Y[j] = bp.Y[j][p];
+        s.p = p, s.T = T0, s.dt = bp.dt[p], s.rho = rho0, s.i = 1;
+        if (phase == 1)
+        {
+            const ResumeState& r = bp.rs;
+            s.elapsed = r.elapsed[p], s.nextT = r.nextT[p], s.drho = r.drho[p], s.nit = r.nit[p];
+            s.nsub = r.nsub[p], s.cdDt = r.cdDt[p], s.cdNt = r.cdNt[p], s.cdPower = r.cdPower[p];
+            s.cdSteps = r.cdSteps[p];
+        }
+        else
+        {
+            double drho = 0;
+            if (bp.useDrhodt && bp.rhoM1 && bp.rhoM1[p] != 0) drho = (rho0 - bp.rhoM1[p]) / bp.previousDt;
+            s.elapsed = 0, s.nextT = 0, s.drho = drho, s.nit = 0, s.nsub = 0;
+            s.cycleReset();
+        }
+        s.nit0 = s.nit;
+        __syncwarp();
+
+        // ---- Newton iterations of this particle
+        int st;
+        for (;;)
+        {
+            if (s.nit >= bp.maxIter)
+            {
+                st = ST_MAXITER;
+                break;
+            }
+            if (bp.sliceIters > 0 && s.i == 1 && s.nit - s.nit0 >= bp.sliceIters)
+            {
+                st = kPaused;
+                break;
+            }
+            const double dtTot = bp.hydroDt;
+            const double rhoT  = s.rho - s.drho * (dtTot - s.elapsed);
+            double       used  = s.dt;
+            if (dtTot - s.elapsed < s.dt) used = dtTot - s.elapsed;
+            if (used == 0)
+            {
+                st = ST_ZERO_DT;
+                break;
+            }
+            ++s.nit;
+            const double guessT = s.i <= 1 ? s.T : s.nextT;
+            const double Ttheta = (1 - k::theta) * s.T + k::theta * guessT;
+            double       ab = 0, zb = 0;
+            for (int j = lane; j < D::N; j += 32)
+            {
+                const double y  = S.Y[j];
+                const double yn = (1 - k::theta) * y + k::theta * (s.i <= 1 ? y : S.Yn[j]);
+                S.Yn[j]         = yn;
+                ab += yn, zb += yn * __ldg(nv.Z + j);
+            }
+            __syncwarp();
+            EosResult eos;
+            if constexpr (EOS == NNET_EOS_IDEAL_GAS)
+                eos = idealGasEos(bp.mu, Ttheta, rhoT);
+            else
+                eos = helmholtzEos(hv, warpSum(ab), warpSum(zb), Ttheta, rhoT);
+
+            warpRates<NET, MIXED>(nv, S, Ttheta, rhoT, lane);
+            warpAssemble<NET, MIXED>(nv, S, s.T, Ttheta, rhoT, s.drho, eos.cv, eos.dpdT, used, lane);
+            if constexpr (MIXED)
+            {
+                const int steps = warpSolveMixed<NET>(nv, S, s.T, lane, S.scale);
+                if (steps < 0)
+                {
+                    // not settled: re-solve this system in FP64 (A and b are intact)
+                    warpSolve64<NET, MIXED>(nv, S, lane);
+                    if (lane == 0) atomicAdd(bp.stats + 8, 1ull);
+                }
+                else if (steps && lane == 0)
+                    atomicAdd(bp.stats + 7, (unsigned long long)steps);
+            }
+            else
+                warpSolve64<NET, MIXED>(nv, S, lane);
+
+            // ---- finalizeSystemSubstep / finalizeSystemNR (nuclear_net.hpp:724-782, :887-922)
+            double usedDt = s.dt;
+            if (dtTot - s.elapsed < s.dt) usedDt = dtTot - s.elapsed;
+            const double lastT = s.nextT, T = s.T;
+            bool         nanl  = false;
+            for (int j = lane; j < D::N; j += 32)
+            {
+                const double v = S.Y[j] + S.x[__ldg(sp.iperm + j + 1)];
+                S.Yn[j]        = v;
+                nanl |= isnan(v);
+            }
+            const bool nan = __any_sync(kFull, nanl);
+            s.nextT        = T + S.x[sp.tNew];
+            __syncwarp();
+            int    iNext    = s.i;
+            bool   conv     = false;
+            double timestep = 0;
+            if (nan || isnan(s.nextT) || s.nextT < 0)
+            {
+                usedDt *= k::nanDtStep;
+                iNext = 0;
+            }
+            else
+            {
+                const double dT_T = fabs((s.nextT - T) / s.nextT);
+                if (s.i >= k::nrMinIt && dT_T > k::nrDTTarget * k::nrDTTol)
+                {
+                    usedDt *= k::nrDTTol / dT_T;
+                    iNext = 0;
+                    for (int j = lane; j < D::N; j += 32)
+                        S.Yn[j] = S.Y[j];
+                    s.nextT = T;
+                }
+                else
+                {
+                    for (int j = lane; j < D::N; j += 32)
+                        if (S.Yn[j] <= k::epsilonVector) S.Yn[j] = 0;
+                    const double correction = fabs((s.nextT - lastT) / s.nextT);
+                    if ((s.i >= k::nrMinIt && correction < k::nrItTol) || s.i >= k::nrMaxIt)
+                    {
+                        const double dTT = fabs((s.nextT - T) / s.nextT);
+                        timestep         = usedDt;
+                        usedDt           = (dTT == 0 ? k::maxDtStep : k::nrDTTarget / dTT) * timestep;
+                        usedDt           = fmin(usedDt, timestep * k::maxDtStep);
+                        usedDt           = fmax(usedDt, timestep * k::minDtStep);
+                        usedDt           = fmin(usedDt, k::nrMaxDt);
+                        conv             = true;
+                    }
+                }
+            }
+            if (dtTot - s.elapsed < s.dt)
+            {
+                if (usedDt < dtTot - s.elapsed) s.dt = usedDt;
+            }
+            else
+                s.dt = usedDt;
+            __syncwarp();
+            if (conv)
+            {
+                for (int j = lane; j < D::N; j += 32)
+                    S.Y[j] = S.Yn[j];
+                __syncwarp();
+                s.T = s.nextT;
+                s.elapsed += timestep;
+                ++s.nsub;
+                s.i = 1;
+                if ((dtTot - s.elapsed) / dtTot < k::substepDtTol)
+                {
+                    st = ST_OK;
+                    break;
+                }
+                s.cycleReset();
+                continue;
+            }
+            if (iNext == 0)
+            {
+                if (s.cycleRejected())
+                {
+                    st = ST_LIVELOCK;
+                    break;
+                }
+                s.i = 1;
+                continue;
+            }
+            s.i = iNext + 1;
+        }
+
+        // ---- write back (pause or finish)
+        for (int j = lane; j < D::N; j += 32)
+            bp.Y[j][p] = S.Y[j];
+        __syncwarp();
+        if (lane == 0)
+        {
+            bp.T[p]  = s.T;
+            bp.dt[p] = s.dt;
+            atomicAdd(bp.stats + 0, (unsigned long long)(s.nit - s.nit0));
+            if (st == kPaused)
+            {
+                const ResumeState& r = bp.rs;
+                r.elapsed[p] = s.elapsed, r.nextT[p] = s.nextT, r.drho[p] = s.drho, r.nit[p] = s.nit;
+                r.nsub[p] = s.nsub, r.cdDt[p] = s.cdDt, r.cdNt[p] = s.cdNt, r.cdPower[p] = s.cdPower;
+                r.cdSteps[p] = s.cdSteps, r.phase[p] = 1;
+            }
+            else
+            {
+                if (bp.status) bp.status[p] = st;
+                if (bp.substeps) bp.substeps[p] = s.nsub;
+                if (bp.iterations) bp.iterations[p] = (int32_t)s.nit;
+                atomicAdd(bp.stats + 1, (unsigned long long)s.nsub);
+                atomicAdd(bp.stats + 2 + st, 1ull);
+                finishSegment(bp, p);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+template<int NET, int EOS, bool MIXED>
+static KernelInfo warpInfo()
+{
+    return {(const void*)burnWarpKernel<NET, EOS, MIXED>, 0, 128, WDims<NET>::NNZ,
+            4 * WarpSmem<NET, MIXED>::doubles * sizeof(double)};
+}
+
+template<bool MIXED>
+static KernelInfo pickWarp(int net, int eos)
+{
+    if (net == 14) return eos ? warpInfo<14, 1, MIXED>() : warpInfo<14, 0, MIXED>();
+    if (net == 86) return eos ? warpInfo<86, 1, MIXED>() : warpInfo<86, 0, MIXED>();
+    return eos ? warpInfo<87, 1, MIXED>() : warpInfo<87, 0, MIXED>();
+}
+
+KernelInfo warpKernel(int net, int eos, int mixed) { return mixed ? pickWarp<true>(net, eos) : pickWarp<false>(net, eos); }
+
+} // namespace nnet_gb300

@@ -53,6 +53,15 @@ struct SparseView
     const double* cCoef;
 };
 
+// Device view of a network's warp-per-particle lists (see WarpPlan in sparse_plan.hpp)
+struct WarpView
+{
+    int           nJ, nEnt, nSgHeavy, nJgHeavy, nRjHeavy, nRowHeavy;
+    const int *   updBeg, *updT, *updL, *updU, *ucBeg, *ucPos, *ucRow, *sgBeg, *sgRx, *jPos, *jRow, *jCol, *jgBeg,
+        *jgEnt, *rjBeg, *rjEnt, *entRx, *sgHeavy, *jgHeavy, *rjHeavy, *rowHeavy;
+    const double *sgCoef, *jgCoef;
+};
+
 // Read-only device view of one network definition (reaction list in CSR form, binding
 // energies, charges, fit / partition-function tables).
 struct NetView
@@ -66,6 +75,7 @@ struct NetView
     const int *   mainReactant, *secondaryReactant, *mainProduct;
     const double *eLogT, *eLogRho, *eRate;
     SparseView    sp;
+    WarpView      wv;
 };
 
 // Helmholtz table: one 128-byte line per grid cell (i, j) holding the 13 quantities the

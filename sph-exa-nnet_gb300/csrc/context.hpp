@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include "common.cuh"
+#include "launch.hpp"
 #include "sparse_plan.hpp"
 
 namespace nnet_gb300
@@ -34,6 +35,9 @@ struct Workspace
 int launchBurn(struct ::nnet_context* h, const nnet_burn_args* args, Workspace& ws, cudaStream_t st,
                const ResumeState* rs, long long sliceIters, unsigned long long* segFinished);
 
+// kernel of (network, eos, solver) under the context's layout
+KernelInfo burnKernel(struct ::nnet_context* h, int net, int eos, int solver);
+
 // scratch doubles of the largest persistent grid of any network for `solver`
 size_t maxScratchDoubles(struct ::nnet_context* h, int solver);
 
@@ -49,4 +53,5 @@ struct nnet_context
     nnet_gb300::Workspace  ws;
     cudaStream_t           lastStream = nullptr;
     bool                   lastMulti  = false; // last launch was nnet_burn_batch
+    int                    layout     = NNET_LAYOUT_AUTO;
 };

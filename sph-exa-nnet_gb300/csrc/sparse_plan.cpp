@@ -145,3 +145,106 @@ SparsePlan buildSparsePlan(int net, const int* rbeg, const int* rspec, const int
 }
 
 } // namespace nnet_gb300
+
+namespace nnet_gb300
+{
+
+WarpPlan buildWarpPlan(const SparsePlan& P, const int* rbeg, const int* rspec, const int* rcnt, const int* pbeg,
+                       const int* pspec, const int* pcnt)
+{
+    WarpPlan  W;
+    const int n = P.n, N = P.N, R = P.R;
+    // flat factorisation updates
+    W.updBeg.push_back(0);
+    for (int k = 0; k < n; ++k)
+    {
+        const int nu = P.uBeg[k + 1] - P.uBeg[k];
+        for (int e = P.lBeg[k]; e < P.lBeg[k + 1]; ++e)
+            for (int u = 0; u < nu; ++u)
+            {
+                W.updT.push_back(P.tPos[P.tBeg[e] + u]);
+                W.updL.push_back(P.lPos[e]);
+                W.updU.push_back(P.uPos[P.uBeg[k] + u]);
+            }
+        W.updBeg.push_back((int)W.updT.size());
+    }
+    // U by columns
+    std::vector<std::vector<std::pair<int, int>>> cols(n);
+    for (int k = 0; k < n; ++k)
+        for (int u = P.uBeg[k]; u < P.uBeg[k + 1]; ++u)
+            cols[P.uCol[u]].push_back({P.uPos[u], k});
+    W.ucBeg.push_back(0);
+    for (int c = 0; c < n; ++c)
+    {
+        for (auto& pr : cols[c])
+            W.ucPos.push_back(pr.first), W.ucRow.push_back(pr.second);
+        W.ucBeg.push_back((int)W.ucPos.size());
+    }
+    // species gathers (reactant: -count, product: +count), in reaction order
+    std::vector<std::vector<std::pair<int, double>>> sg(N);
+    for (int r = 0; r < R; ++r)
+    {
+        for (int k = rbeg[r]; k < rbeg[r + 1]; ++k)
+            sg[rspec[k]].push_back({r, -(double)rcnt[k]});
+        for (int k = pbeg[r]; k < pbeg[r + 1]; ++k)
+            sg[pspec[k]].push_back({r, (double)pcnt[k]});
+    }
+    W.sgBeg.push_back(0);
+    for (int s = 0; s < N; ++s)
+    {
+        for (auto& pr : sg[s])
+            W.sgRx.push_back(pr.first), W.sgCoef.push_back(pr.second);
+        W.sgBeg.push_back((int)W.sgRx.size());
+    }
+    // Jacobian entries and their gathers, from the contribution list of the sparse plan
+    std::vector<int> entryOf(P.nnz, -1);
+    std::vector<std::vector<std::pair<int, double>>> jg;
+    for (int e = 0; e < rbeg[R]; ++e)
+        for (int c = P.cBeg[e]; c < P.cBeg[e + 1]; ++c)
+        {
+            const int pos = P.cPos[c];
+            if (entryOf[pos] < 0)
+            {
+                entryOf[pos] = (int)W.jPos.size();
+                W.jPos.push_back(pos);
+                W.jRow.push_back(P.cRow[c]);
+                W.jCol.push_back(rspec[e]);
+                jg.emplace_back();
+            }
+            jg[entryOf[pos]].push_back({e, P.cCoef[c]});
+        }
+    W.jgBeg.push_back(0);
+    for (auto& l : jg)
+    {
+        for (auto& pr : l)
+            W.jgEnt.push_back(pr.first), W.jgCoef.push_back(pr.second);
+        W.jgBeg.push_back((int)W.jgEnt.size());
+    }
+    std::vector<std::vector<int>> rows(N);
+    for (int m = 0; m < (int)W.jPos.size(); ++m)
+        rows[W.jRow[m]].push_back(m);
+    W.rjBeg.push_back(0);
+    for (int i = 0; i < N; ++i)
+    {
+        std::sort(rows[i].begin(), rows[i].end(), [&](int a, int b) { return W.jCol[a] < W.jCol[b]; });
+        for (int m : rows[i])
+            W.rjEnt.push_back(m);
+        W.rjBeg.push_back((int)W.rjEnt.size());
+    }
+    W.entRx.assign(rbeg[R], 0);
+    for (int r = 0; r < R; ++r)
+        for (int k = rbeg[r]; k < rbeg[r + 1]; ++k)
+            W.entRx[k] = r;
+    for (int s = 0; s < N; ++s)
+        if (W.sgBeg[s + 1] - W.sgBeg[s] > WarpPlan::kHeavy) W.sgHeavy.push_back(s);
+    for (int m = 0; m + 1 < (int)W.jgBeg.size(); ++m)
+        if (W.jgBeg[m + 1] - W.jgBeg[m] > WarpPlan::kHeavy) W.jgHeavy.push_back(m);
+    for (int i = 0; i < N; ++i)
+        if (W.rjBeg[i + 1] - W.rjBeg[i] > WarpPlan::kHeavy) W.rjHeavy.push_back(i);
+    for (int i = 0; i < n; ++i)
+        if (P.rowBeg[i + 1] - P.rowBeg[i] > WarpPlan::kHeavy) W.rowHeavy.push_back(i);
+    (void)pspec, (void)pcnt, (void)rcnt;
+    return W;
+}
+
+} // namespace nnet_gb300

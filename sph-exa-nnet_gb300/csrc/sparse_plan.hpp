@@ -44,4 +44,34 @@ struct SparsePlan
 SparsePlan buildSparsePlan(int net, const int* rbeg, const int* rspec, const int* rcnt, const int* pbeg,
                            const int* pspec, const int* pcnt, int R);
 
+// Extra lists of the warp-per-particle kernels, in which the 32 lanes of a warp share one
+// particle's Newton system in shared memory.  Accumulations are written as gathers (each
+// target sums its own contribution list in a fixed order) so that no two lanes write the
+// same word and results are deterministic; a list longer than kHeavy (the p, n, alpha rows
+// and columns of net86) is summed by the whole warp with a fixed butterfly reduction.
+struct WarpPlan
+{
+    static constexpr int kHeavy = 16;
+    // factorisation updates of pivot k: updBeg[k] .. updBeg[k+1], target / L / U positions
+    std::vector<int> updBeg, updT, updL, updU;
+    // column k of U above the diagonal (column-oriented backward substitution)
+    std::vector<int> ucBeg, ucPos, ucRow;
+    // species gathers of dY/dt: species s sums coef * flux[reaction] over sgBeg[s]..sgBeg[s+1]
+    std::vector<int>    sgBeg, sgRx;
+    std::vector<double> sgCoef;
+    // Jacobian gathers: J entry m (position jPos[m], species row jRow[m], species column
+    // jCol[m]) sums coef * tr[reactant entry] over jgBeg[m]..jgBeg[m+1]
+    std::vector<int>    jPos, jRow, jCol, jgBeg, jgEnt;
+    std::vector<double> jgCoef;
+    // J entries of species row i: rjBeg[i] .. rjBeg[i+1] (indices into the J entry list)
+    std::vector<int> rjBeg, rjEnt;
+    // reaction of every reactant entry
+    std::vector<int> entRx;
+    // targets whose lists are longer than kHeavy (summed by the whole warp)
+    std::vector<int> sgHeavy, jgHeavy, rjHeavy, rowHeavy; // species, J entries, J rows, factor rows
+};
+
+WarpPlan buildWarpPlan(const SparsePlan& P, const int* rbeg, const int* rspec, const int* rcnt, const int* pbeg,
+                       const int* pspec, const int* pcnt);
+
 } // namespace nnet_gb300

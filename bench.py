@@ -39,14 +39,14 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--solver", default=None)
     ap.add_argument("--particles", type=int, default=1048576)
-    ap.add_argument("--plain-particles", type=int, default=131072,
+    ap.add_argument("--plain-particles", type=int, default=4096,
                     help="particles of the plain FP64 comparison leg (0 disables it)")
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--cpu-sample", type=int, default=4096)
     ap.add_argument("--max-iter", type=int, default=20000)
     ap.add_argument("--serve-requests", type=int, default=48,
                     help="requests of the served-stream leg (0 disables it)")
-    ap.add_argument("--serve-plain-requests", type=int, default=12,
+    ap.add_argument("--serve-plain-requests", type=int, default=8,
                     help="requests of the plain-FP64 served-stream comparison (0 disables it)")
     return ap.parse_args()
 
@@ -170,7 +170,7 @@ def main():
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     ctx = nn.Context(local)
-    solver = args.solver or "mixed"
+    solver = args.solver or "sparse"
     sv = nn.SOLVERS[solver]
 
     # ---- device-resident workload (this rank's shard)
@@ -263,6 +263,14 @@ def main():
         p1.record(stream)
         barrier()
         plain = {"value": Pp / (p0.elapsed_time(p1) / 1e3), "unit": UNIT, "particles": Pp}
+        # the fast form on the same sub-batch (same occupancy as the plain measurement)
+        Y[:, sl].copy_(Y0[:, sl]), T[sl].copy_(T0[sl]), dt[sl].copy_(dt0[sl])
+        p0.record(stream)
+        ctx.burn(86, Y[:, sl], T[sl], rho[sl], dt[sl], w["hydro_dt"], eos=nn.EOS_HELMHOLTZ, solver=sv,
+                 max_iter=args.max_iter, stream=stream)
+        p1.record(stream)
+        barrier()
+        plain["fast_form_same_particles"] = Pp / (p0.elapsed_time(p1) / 1e3)
 
     # ---- roofline: FP64 pipe (the kernel computes in FP64; no HBM or tensor bound applies)
     iters = stats["newton_iterations"]
@@ -291,9 +299,13 @@ def main():
     if plain:
         line["plain_fp64"] = plain
     if args.serve_requests and rank == 0:
-        line["serving"] = serve_bench(nn, ctx, "mixed" if solver != "dense" else "dense", args.serve_requests, 5)
+        line["serving"] = serve_bench(nn, ctx, solver, args.serve_requests, 5)
         if args.serve_plain_requests and solver != "dense":
-            line["serving_plain_fp64"] = serve_bench(nn, ctx, "dense", args.serve_plain_requests, 5)
+            # the plain form serves about 1/300 of the fast form's rate: both forms on the same
+            # stream with request sizes divided by 128
+            line["serving_small_stream"] = {
+                "fast": serve_bench(nn, ctx, solver, args.serve_plain_requests, 6, scale=128),
+                "plain_fp64": serve_bench(nn, ctx, "dense", args.serve_plain_requests, 6, scale=128)}
     if rank == 0:
         try:
             v, el, thr = cpu_burn_rate(args.cpu_sample)
@@ -307,14 +319,14 @@ def main():
         dist.destroy_process_group()
 
 
-def serve_requests(n, seed):
+def serve_requests(n, seed, scale=1):
     """Served burn stream: Poisson arrivals (mean 200/s), sizes log-uniform 1k-500k
-    particles, network tag uniform over net14/net86/net87, states drawn from the c2
-    (net86/net87 with Y_e = 0.5, net14 with the same composition) distributions."""
+    particles (divided by `scale`), network tag uniform over net14/net86/net87, states drawn
+    from the c2 (net86/net87 with Y_e = 0.5, net14 with the same composition) distributions."""
     import workloads
     rng = np.random.default_rng(seed)
     gaps = rng.exponential(1 / 200.0, n)
-    sizes = np.exp(rng.uniform(np.log(1e3), np.log(5e5), n)).astype(int)
+    sizes = np.maximum(np.exp(rng.uniform(np.log(1e3), np.log(5e5), n)) / scale, 1).astype(int)
     nets = rng.choice([14, 86, 87], n)
     reqs = []
     for k in range(n):
@@ -327,11 +339,11 @@ def serve_requests(n, seed):
     return reqs
 
 
-def serve_bench(nn, ctx, solver, n, seed):
+def serve_bench(nn, ctx, solver, n, seed, scale=1):
     """Submit the stream with its arrival gaps to a continuous-batching server (150 GB
     HBM budget) and report served particle-burns/s and request latency percentiles."""
     import torch
-    reqs = serve_requests(n, seed)
+    reqs = serve_requests(n, seed, scale)
     pinned = []
     for r in reqs:  # pinned host buffers: asynchronous copies
         arrs = [torch.from_numpy(np.ascontiguousarray(r[k])).pin_memory() for k in ("Y", "T", "rho", "dt")]
@@ -352,7 +364,7 @@ def serve_bench(nn, ctx, solver, n, seed):
     return {"solver": solver, "requests": n, "particles": particles, "value": particles / wall, "unit": UNIT,
             "wall_s": wall, "latency_p50_s": float(np.percentile(lat, 50)),
             "latency_p95_s": float(np.percentile(lat, 95)), "latency_p99_s": float(np.percentile(lat, 99)),
-            "offered_load": "Poisson 200/s, sizes log-uniform 1e3-5e5, nets uniform {14,86,87}",
+            "offered_load": f"Poisson 200/s, sizes log-uniform 1e3-5e5 / {scale}, nets uniform {{14,86,87}}",
             "slices": st["slices"]}
 
 

@@ -1313,6 +1313,27 @@ int oracle_helm_eos_batch(size_t P, int dim, const double* Z, const double* T, c
     return 0;
 }
 
+// The Newton system of the first iteration of a substep from state (Y, T) with step dt, as
+// M (column-major: M[i + (N+1) j] is element (i, j); index 0 = temperature) and RHS;
+// for analysis of the linear solves.
+int oracle_newton_system(int net, int eos_kind, double mu, const double* Y, double T, double rho, double drho_dt,
+                         double dt, double* M, double* RHS)
+{
+    Ctx c{net, 0, eos_kind, mu, {}};
+    if (!getNetwork(net, c.n)) return -1;
+    c.dim = c.n.nspec;
+    Work               w(c.dim, c.n.nreact);
+    std::vector<double> Yg(Y, Y + c.dim);
+    const Eos          e = computeEos(c, Yg.data(), T, rho);
+    prepareFromGuess(c, w.Mp.data(), w.RHS.data(), w.rates.data(), Y, T, Yg.data(), T, rho, drho_dt, e, dt);
+    const int ld = c.dim + 1;
+    for (int i = 0; i < ld * ld; ++i)
+        M[i] = w.Mp[i];
+    for (int i = 0; i < ld; ++i)
+        RHS[i] = w.RHS[i];
+    return 0;
+}
+
 // Single-particle Newton solve without substepping (nuclear_net.hpp:791-818)
 double oracle_solve_nr(int net, int eos_kind, double mu, const double* Y, double T, double* Y_out, double* T_out,
                        double rho, double drho_dt, double* dt)

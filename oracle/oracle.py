@@ -44,6 +44,11 @@ class Oracle:
         self._nr.argtypes = [_I, _I, _D, _P, _D, _P, _P, _D, _D, _P]
         self._nr.restype = _D
         try:
+            self._sys = g("newton_system")
+            self._sys.argtypes = [_I, _I, _D, _P, _D, _D, _D, _D, _P, _P]
+        except AttributeError:
+            self._sys = None
+        try:
             self._eosb = g("helm_eos_batch")
             self._eosb.argtypes = [_S, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _I]
         except AttributeError:
@@ -86,6 +91,17 @@ class Oracle:
         Yo, To, d = np.zeros(net), np.zeros(1), np.array([dt], dtype=np.float64)
         ts = self._nr(net, 0 if eos == "ideal" else 1, mu, _ptr(Y), T, _ptr(Yo), _ptr(To), rho, drho_dt, _ptr(d))
         return Yo, float(To[0]), float(d[0]), ts
+
+    def newton_system(self, net, Y, T, rho, dt, eos="ideal", mu=10.0, drho_dt=0.0):
+        """(A, b) of the first Newton iteration of a substep from (Y, T) with step dt;
+        index 0 is the temperature, 1.. the species."""
+        Y = np.ascontiguousarray(Y, dtype=np.float64)
+        n = net + 1
+        M, b = np.zeros(n * n), np.zeros(n)
+        rc = self._sys(net, 0 if eos == "ideal" else 1, mu, _ptr(Y), T, rho, drho_dt, dt, _ptr(M), _ptr(b))
+        if rc:
+            raise RuntimeError("newton_system failed")
+        return M.reshape(n, n).T.copy(), b
 
     def helm_eos_batch(self, Z, T, rho, Y, nthreads=0):
         Y = np.ascontiguousarray(Y, dtype=np.float64)

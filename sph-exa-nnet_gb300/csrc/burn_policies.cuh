@@ -447,7 +447,7 @@ struct SparsePolicy
                 const double di = (double)d32[i], xi = x[i] + di;
                 const int    o  = __ldg(sp.perm + i); // reference index: 0 = T, 1.. = species
                 const double sc = o == 0 ? T : fabs(Y[o - 1]);
-                conv &= fabs(di) <= kRefineTol * (fabs(xi) + sc);
+                conv &= fabs(di) <= kRefineTol * (fabs(xi) + sc) && isfinite(xi); // an FP32 overflow is not convergence
                 x[i] = xi;
             }
             if (conv) return steps;

@@ -466,7 +466,7 @@ __device__ int warpSolveMixed(const NetView& nv, WarpSmem<NET, true>& S, double 
             const double di = (double)S.d[i], xi = S.x[i] + di;
             const int    o  = __ldg(sp.perm + i);
             const double sc = o == 0 ? T : fabs(S.Y[o - 1]);
-            conv &= fabs(di) <= kRefineTol * (fabs(xi) + sc);
+            conv &= fabs(di) <= kRefineTol * (fabs(xi) + sc) && isfinite(xi); // an FP32 overflow is not convergence
             S.x[i] = xi;
         }
         conv = __all_sync(kFull, conv);

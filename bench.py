@@ -42,7 +42,7 @@ def parse():
     ap.add_argument("--plain-particles", type=int, default=4096,
                     help="particles of the plain FP64 comparison leg (0 disables it)")
     ap.add_argument("--impl", default="gb300")
-    ap.add_argument("--cpu-sample", type=int, default=4096)
+    ap.add_argument("--cpu-sample", type=int, default=32768)
     ap.add_argument("--max-iter", type=int, default=20000)
     ap.add_argument("--serve-requests", type=int, default=48,
                     help="requests of the served-stream leg (0 disables it)")
@@ -291,7 +291,9 @@ def main():
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": args.steps,
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                         "frac": achieved / peak, "traffic": None,
+                         "frac": achieved / peak, "traffic": TRAFFIC_PER_PARTICLE * P,
+                         "traffic_source": "dram read+write of one ncu capture (32,768 particles), "
+                                           "scaled by the particles of one launch",
                          "peak_source": peak_src + "; MEASURED_PEAKS.json has no FP64 figure",
                          "flops_per_newton_iteration": flops_per_iter,
                          "refinement_steps": stats["refinement_steps"], "fp64_fallbacks": stats["fp64_fallbacks"]},
@@ -384,6 +386,9 @@ def algorithmic_flops(nn, net, solver):
 
 
 FP64_PEAK_TFLOPS = 1.25
+# dram__bytes_read.sum + dram__bytes_write.sum of burnWarpKernel<86, Helmholtz> on 32,768 c2
+# particles (24.68 MB + 0.08 MB): the particle state, read once; tables stay in L2
+TRAFFIC_PER_PARTICLE = (24.677376e6 + 0.08192e6) / 32768
 
 if __name__ == "__main__":
     main()

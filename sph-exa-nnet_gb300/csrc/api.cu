@@ -120,6 +120,11 @@ int uploadNetwork(int net, NetBuffer& b)
                  oJgB = putv(wp.jgBeg), oJgE = putv(wp.jgEnt), oRjB = putv(wp.rjBeg), oRjE = putv(wp.rjEnt),
                  oERx = putv(wp.entRx), oSgH = putv(wp.sgHeavy), oJgH = putv(wp.jgHeavy), oRjH = putv(wp.rjHeavy),
                  oRowH = putv(wp.rowHeavy);
+    const size_t oLvB = putv(wp.lvBeg), oLvP = putv(wp.lvPiv), oLsB = putv(wp.lsBeg), oLsP = putv(wp.lsPos),
+                 oLsK = putv(wp.lsPiv), oTgB = putv(wp.tgBeg), oTgP = putv(wp.tgPos), oTgU = putv(wp.tgUpd),
+                 oTuL = putv(wp.tuL), oTuU = putv(wp.tuU), oFwB = putv(wp.fwBeg), oFwR = putv(wp.fwRow),
+                 oFwE = putv(wp.fwEnt), oFlP = putv(wp.flPos), oFlK = putv(wp.flK), oBwB = putv(wp.bwBeg),
+                 oBwR = putv(wp.bwRow), oBwE = putv(wp.bwEnt), oBuP = putv(wp.buPos), oBuK = putv(wp.buK);
     const size_t bytesD = d.size() * sizeof(double), bytes = bytesD + ii.size() * sizeof(int);
     NNET_CUDA(cudaMalloc(&b.mem, bytes));
     NNET_CUDA(cudaMemcpy(b.mem, d.data(), bytesD, cudaMemcpyHostToDevice));
@@ -148,6 +153,11 @@ int uploadNetwork(int net, NetBuffer& b)
     x.jCol = I + oJC, x.jgBeg = I + oJgB, x.jgEnt = I + oJgE, x.rjBeg = I + oRjB, x.rjEnt = I + oRjE;
     x.entRx = I + oERx, x.sgHeavy = I + oSgH, x.jgHeavy = I + oJgH, x.rjHeavy = I + oRjH, x.rowHeavy = I + oRowH;
     x.sgCoef = D + oSgC, x.jgCoef = D + oJgC;
+    x.nLevels = wp.nLevels;
+    x.lvBeg = I + oLvB, x.lvPiv = I + oLvP, x.lsBeg = I + oLsB, x.lsPos = I + oLsP, x.lsPiv = I + oLsK;
+    x.tgBeg = I + oTgB, x.tgPos = I + oTgP, x.tgUpd = I + oTgU, x.tuL = I + oTuL, x.tuU = I + oTuU;
+    x.fwBeg = I + oFwB, x.fwRow = I + oFwR, x.fwEnt = I + oFwE, x.flPos = I + oFlP, x.flK = I + oFlK;
+    x.bwBeg = I + oBwB, x.bwRow = I + oBwR, x.bwEnt = I + oBwE, x.buPos = I + oBuP, x.buK = I + oBuK;
     return NNET_SUCCESS;
 }
 

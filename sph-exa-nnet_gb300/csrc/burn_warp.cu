@@ -49,12 +49,12 @@ struct WarpSmem
     static constexpr int oY = 0, oYn = oY + D::N, oF = oYn + D::N, oDF = oF + D::R, oBE = oDF + D::R,
                          oA = oBE + D::N, oB = oA + D::NNZ, oDYdt = oB + D::n, oDYdT = oDYdt + D::N,
                          oJdy = oDYdT + D::N, oTr = oJdy + D::N;
-    static constexpr int floatsD = (D::NNZ + D::n + 1) / 2;
+    static constexpr int floatsD = (D::NNZ + 2 * D::n + 1) / 2;
     static constexpr int doubles = oTr + (MIXED && floatsD > D::NE ? floatsD : D::NE);
 
     static_assert(4 * D::n <= 2 * D::R + D::N, "solve vectors must fit the flux storage");
     double *Y, *Yn, *f, *df, *BE, *A, *b, *dYdt, *mu, *dYdT, *jdy, *tr, *x, *r, *ipiv, *scale;
-    float * LU, *d;
+    float * LU, *d, *ipiv32;
 
     __device__ explicit WarpSmem(double* s)
     {
@@ -63,7 +63,7 @@ struct WarpSmem
         mu = dYdt; // screening potentials live until the rates are done
         // the solve vectors reuse the flux / binding-energy storage, dead after assembly
         x = f, r = f + D::n, ipiv = f + 2 * D::n, scale = f + 3 * D::n;
-        LU = reinterpret_cast<float*>(tr), d = LU + D::NNZ;
+        LU = reinterpret_cast<float*>(tr), d = LU + D::NNZ, ipiv32 = d + D::n;
     }
 };
 
@@ -338,83 +338,83 @@ __device__ void warpAssemble(const NetView& nv, WarpSmem<NET, MIXED>& S, double 
 }
 
 // ------------------------------------------------------------------ solves (warp)
-// FP64: factor A in place, x = A^-1 b (x aliases nothing the factor uses)
-template<int NET, bool MIXED>
-__device__ void warpSolve64(const NetView& nv, WarpSmem<NET, MIXED>& S, int lane)
+// Level-scheduled right-looking LU without pivoting, in place (FP64 or FP32): per level,
+// the pivots' reciprocals, then their multipliers, then every target's updates in pivot order.
+__device__ __forceinline__ double recip(double a) { return __drcp_rn(a); }
+__device__ __forceinline__ float  recip(float a) { return __frcp_rn(a); }
+
+template<typename F>
+__device__ void levelFactor(const SparseView& sp, const WarpView& wv, F* A, F* ipiv, int lane)
 {
-    using D              = WDims<NET>;
-    const SparseView& sp = nv.sp;
-    const WarpView&   wv = nv.wv;
-    for (int k = 0; k < D::n; ++k)
+    for (int l = 0; l < wv.nLevels; ++l)
     {
-        const double ip = __drcp_rn(S.A[__ldg(sp.kPiv + k)]);
-        for (int e = __ldg(sp.lBeg + k) + lane; e < __ldg(sp.lBeg + k + 1); e += 32)
-            S.A[__ldg(sp.lPos + e)] *= ip;
-        if (lane == 0) S.ipiv[k] = ip;
-        __syncwarp();
-        for (int q = __ldg(wv.updBeg + k) + lane; q < __ldg(wv.updBeg + k + 1); q += 32)
+        for (int q = __ldg(wv.lvBeg + l) + lane; q < __ldg(wv.lvBeg + l + 1); q += 32)
         {
-            const int t = __ldg(wv.updT + q);
-            S.A[t]      = S.A[t] - S.A[__ldg(wv.updL + q)] * S.A[__ldg(wv.updU + q)];
+            const int k = __ldg(wv.lvPiv + q);
+            ipiv[k]     = recip(A[__ldg(sp.kPiv + k)]);
         }
         __syncwarp();
-    }
-    for (int i = lane; i < D::n; i += 32)
-        S.x[i] = S.b[i];
-    __syncwarp();
-    for (int k = 0; k < D::n; ++k)
-    {
-        const double bk = S.x[k];
-        for (int e = __ldg(sp.lBeg + k) + lane; e < __ldg(sp.lBeg + k + 1); e += 32)
-        {
-            const int i = __ldg(sp.lRow + e);
-            S.x[i]      = S.x[i] - S.A[__ldg(sp.lPos + e)] * bk;
-        }
+        for (int e = __ldg(wv.lsBeg + l) + lane; e < __ldg(wv.lsBeg + l + 1); e += 32)
+            A[__ldg(wv.lsPos + e)] *= ipiv[__ldg(wv.lsPiv + e)];
         __syncwarp();
-    }
-    for (int k = D::n - 1; k >= 0; --k)
-    {
-        const double xk = S.x[k] * S.ipiv[k];
-        __syncwarp();
-        if (lane == 0) S.x[k] = xk;
-        for (int q = __ldg(wv.ucBeg + k) + lane; q < __ldg(wv.ucBeg + k + 1); q += 32)
+        for (int t = __ldg(wv.tgBeg + l) + lane; t < __ldg(wv.tgBeg + l + 1); t += 32)
         {
-            const int i = __ldg(wv.ucRow + q);
-            S.x[i]      = S.x[i] - S.A[__ldg(wv.ucPos + q)] * xk;
+            const int pos = __ldg(wv.tgPos + t);
+            F         a   = A[pos];
+            for (int u = __ldg(wv.tgUpd + t), ue = __ldg(wv.tgUpd + t + 1); u < ue; ++u)
+                a = a - A[__ldg(wv.tuL + u)] * A[__ldg(wv.tuU + u)];
+            A[pos] = a;
         }
         __syncwarp();
     }
 }
 
-// FP32 triangular solves on S.d (in place)
-template<int NET>
-__device__ void warpSolve32(const NetView& nv, WarpSmem<NET, true>& S, int lane)
+// x <- U^-1 L^-1 x with the factor of levelFactor (same level schedule)
+template<typename F>
+__device__ void levelSolve(const WarpView& wv, const F* A, const F* ipiv, F* x, int lane)
 {
-    using D              = WDims<NET>;
-    const SparseView& sp = nv.sp;
-    const WarpView&   wv = nv.wv;
-    for (int k = 0; k < D::n; ++k)
+    for (int l = 0; l < wv.nLevels; ++l)
     {
-        const float bk = S.d[k];
-        for (int e = __ldg(sp.lBeg + k) + lane; e < __ldg(sp.lBeg + k + 1); e += 32)
+        for (int r = __ldg(wv.fwBeg + l) + lane; r < __ldg(wv.fwBeg + l + 1); r += 32)
         {
-            const int i = __ldg(sp.lRow + e);
-            S.d[i]      = S.d[i] - S.LU[__ldg(sp.lPos + e)] * bk;
+            const int row = __ldg(wv.fwRow + r);
+            F         a   = x[row];
+            for (int e = __ldg(wv.fwEnt + r), ee = __ldg(wv.fwEnt + r + 1); e < ee; ++e)
+                a = a - A[__ldg(wv.flPos + e)] * x[__ldg(wv.flK + e)];
+            x[row] = a;
         }
         __syncwarp();
     }
-    for (int k = D::n - 1; k >= 0; --k)
+    for (int li = 0; li < wv.nLevels; ++li)
     {
-        const float xk = S.d[k] * (float)S.ipiv[k];
-        __syncwarp();
-        if (lane == 0) S.d[k] = xk;
-        for (int q = __ldg(wv.ucBeg + k) + lane; q < __ldg(wv.ucBeg + k + 1); q += 32)
+        const int l = wv.nLevels - 1 - li;
+        for (int q = __ldg(wv.lvBeg + l) + lane; q < __ldg(wv.lvBeg + l + 1); q += 32)
         {
-            const int i = __ldg(wv.ucRow + q);
-            S.d[i]      = S.d[i] - S.LU[__ldg(wv.ucPos + q)] * xk;
+            const int k = __ldg(wv.lvPiv + q);
+            x[k]        = x[k] * ipiv[k];
+        }
+        __syncwarp();
+        for (int r = __ldg(wv.bwBeg + li) + lane; r < __ldg(wv.bwBeg + li + 1); r += 32)
+        {
+            const int row = __ldg(wv.bwRow + r);
+            F         a   = x[row];
+            for (int e = __ldg(wv.bwEnt + r), ee = __ldg(wv.bwEnt + r + 1); e < ee; ++e)
+                a = a - A[__ldg(wv.buPos + e)] * x[__ldg(wv.buK + e)];
+            x[row] = a;
         }
         __syncwarp();
     }
+}
+
+// FP64: factor A in place, x = A^-1 b
+template<int NET, bool MIXED>
+__device__ void warpSolve64(const NetView& nv, WarpSmem<NET, MIXED>& S, int lane)
+{
+    levelFactor<double>(nv.sp, nv.wv, S.A, S.ipiv, lane);
+    for (int i = lane; i < WDims<NET>::n; i += 32)
+        S.x[i] = S.b[i];
+    __syncwarp();
+    levelSolve<double>(nv.wv, S.A, S.ipiv, S.x, lane);
 }
 
 // rows scaled by powers of two, FP32 factorisation, FP64 residual refinement; returns
@@ -437,20 +437,7 @@ __device__ int warpSolveMixed(const NetView& nv, WarpSmem<NET, true>& S, double 
     for (int p = lane; p < sp.nnz; p += 32)
         S.LU[p] = (float)(S.A[p] * scale[__ldg(sp.posRow + p)]);
     __syncwarp();
-    for (int k = 0; k < D::n; ++k)
-    {
-        const float ip = 1.f / S.LU[__ldg(sp.kPiv + k)];
-        for (int e = __ldg(sp.lBeg + k) + lane; e < __ldg(sp.lBeg + k + 1); e += 32)
-            S.LU[__ldg(sp.lPos + e)] *= ip;
-        if (lane == 0) S.ipiv[k] = ip;
-        __syncwarp();
-        for (int q = __ldg(wv.updBeg + k) + lane; q < __ldg(wv.updBeg + k + 1); q += 32)
-        {
-            const int t = __ldg(wv.updT + q);
-            S.LU[t]     = S.LU[t] - S.LU[__ldg(wv.updL + q)] * S.LU[__ldg(wv.updU + q)];
-        }
-        __syncwarp();
-    }
+    levelFactor<float>(sp, wv, S.LU, S.ipiv32, lane);
     for (int i = lane; i < D::n; i += 32)
         S.x[i] = 0., S.r[i] = S.b[i];
     __syncwarp();
@@ -459,7 +446,7 @@ __device__ int warpSolveMixed(const NetView& nv, WarpSmem<NET, true>& S, double 
         for (int i = lane; i < D::n; i += 32)
             S.d[i] = (float)(S.r[i] * scale[i]);
         __syncwarp();
-        warpSolve32<NET>(nv, S, lane);
+        levelSolve<float>(wv, S.LU, S.ipiv32, S.d, lane);
         bool conv = true;
         for (int i = lane; i < D::n; i += 32)
         {

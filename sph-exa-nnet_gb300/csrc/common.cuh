@@ -60,6 +60,10 @@ struct WarpView
     const int *   updBeg, *updT, *updL, *updU, *ucBeg, *ucPos, *ucRow, *sgBeg, *sgRx, *jPos, *jRow, *jCol, *jgBeg,
         *jgEnt, *rjBeg, *rjEnt, *entRx, *sgHeavy, *jgHeavy, *rjHeavy, *rowHeavy;
     const double *sgCoef, *jgCoef;
+    // level schedule of the factorisation and solves (WarpPlan::nLevels and its lists)
+    int        nLevels;
+    const int *lvBeg, *lvPiv, *lsBeg, *lsPos, *lsPiv, *tgBeg, *tgPos, *tgUpd, *tuL, *tuU;
+    const int *fwBeg, *fwRow, *fwEnt, *flPos, *flK, *bwBeg, *bwRow, *bwEnt, *buPos, *buK;
 };
 
 // Read-only device view of one network definition (reaction list in CSR form, binding

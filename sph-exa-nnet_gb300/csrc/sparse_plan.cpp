@@ -149,6 +149,81 @@ SparsePlan buildSparsePlan(int net, const int* rbeg, const int* rspec, const int
 namespace nnet_gb300
 {
 
+namespace
+{
+void buildLevels(const SparsePlan& P, WarpPlan& W)
+{
+    const int        n = P.n;
+    std::vector<int> lev(n, 0);
+    for (int k = 0; k < n; ++k)
+    {
+        int l = 0;
+        for (int p = P.rowBeg[k]; p < P.rowBeg[k + 1]; ++p)
+            if (P.posCol[p] < k) l = std::max(l, lev[P.posCol[p]] + 1);
+        for (int p = 0; p < P.nnz; ++p)
+            if (P.posCol[p] == k && P.posRow[p] < k) l = std::max(l, lev[P.posRow[p]] + 1);
+        lev[k] = l;
+    }
+    const int nl = n ? *std::max_element(lev.begin(), lev.end()) + 1 : 0;
+    W.nLevels    = nl;
+    std::vector<std::vector<int>> piv(nl);
+    for (int k = 0; k < n; ++k)
+        piv[lev[k]].push_back(k);
+    W.lvBeg = {0}, W.lsBeg = {0}, W.tgBeg = {0}, W.tgUpd = {0}, W.fwBeg = {0}, W.fwEnt = {0};
+    for (int l = 0; l < nl; ++l)
+    {
+        std::map<int, std::vector<std::pair<int, int>>> tgt; // target -> (L pos, U pos), pivot order
+        std::map<int, std::vector<std::pair<int, int>>> fw;  // row -> (L pos, pivot)
+        for (int k : piv[l])
+        {
+            W.lvPiv.push_back(k);
+            for (int e = P.lBeg[k]; e < P.lBeg[k + 1]; ++e)
+            {
+                W.lsPos.push_back(P.lPos[e]), W.lsPiv.push_back(k);
+                fw[P.lRow[e]].push_back({P.lPos[e], k});
+                for (int u = P.uBeg[k]; u < P.uBeg[k + 1]; ++u)
+                    tgt[P.tPos[P.tBeg[e] + (u - P.uBeg[k])]].push_back({P.lPos[e], P.uPos[u]});
+            }
+        }
+        for (auto& [t, lst] : tgt)
+        {
+            W.tgPos.push_back(t);
+            for (auto& pr : lst)
+                W.tuL.push_back(pr.first), W.tuU.push_back(pr.second);
+            W.tgUpd.push_back((int)W.tuL.size());
+        }
+        for (auto& [r, lst] : fw)
+        {
+            W.fwRow.push_back(r);
+            for (auto& pr : lst)
+                W.flPos.push_back(pr.first), W.flK.push_back(pr.second);
+            W.fwEnt.push_back((int)W.flPos.size());
+        }
+        W.lvBeg.push_back((int)W.lvPiv.size());
+        W.lsBeg.push_back((int)W.lsPos.size());
+        W.tgBeg.push_back((int)W.tgPos.size());
+        W.fwBeg.push_back((int)W.fwRow.size());
+    }
+    // backward: levels last to first; rows above the level's pivots, by U column
+    W.bwBeg = {0}, W.bwEnt = {0};
+    for (int l = nl - 1; l >= 0; --l)
+    {
+        std::map<int, std::vector<std::pair<int, int>>> bw; // row i -> (U pos of (i, k), k)
+        for (int k : piv[l])
+            for (int q = W.ucBeg[k]; q < W.ucBeg[k + 1]; ++q)
+                bw[W.ucRow[q]].push_back({W.ucPos[q], k});
+        for (auto& [r, lst] : bw)
+        {
+            W.bwRow.push_back(r);
+            for (auto& pr : lst)
+                W.buPos.push_back(pr.first), W.buK.push_back(pr.second);
+            W.bwEnt.push_back((int)W.buPos.size());
+        }
+        W.bwBeg.push_back((int)W.bwRow.size());
+    }
+}
+} // namespace
+
 WarpPlan buildWarpPlan(const SparsePlan& P, const int* rbeg, const int* rspec, const int* rcnt, const int* pbeg,
                        const int* pspec, const int* pcnt)
 {
@@ -243,6 +318,7 @@ WarpPlan buildWarpPlan(const SparsePlan& P, const int* rbeg, const int* rspec, c
         if (W.rjBeg[i + 1] - W.rjBeg[i] > WarpPlan::kHeavy) W.rjHeavy.push_back(i);
     for (int i = 0; i < n; ++i)
         if (P.rowBeg[i + 1] - P.rowBeg[i] > WarpPlan::kHeavy) W.rowHeavy.push_back(i);
+    buildLevels(P, W);
     (void)pspec, (void)pcnt, (void)rcnt;
     return W;
 }

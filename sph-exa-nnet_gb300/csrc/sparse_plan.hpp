@@ -69,6 +69,24 @@ struct WarpPlan
     std::vector<int> entRx;
     // targets whose lists are longer than kHeavy (summed by the whole warp)
     std::vector<int> sgHeavy, jgHeavy, rjHeavy, rowHeavy; // species, J entries, J rows, factor rows
+
+    // Level schedule: pivot k depends on pivot j < k when (k, j) or (j, k) is stored; the
+    // pivots of one level are mutually independent, so a level's reciprocals, multipliers
+    // and updates run as three warp-parallel rounds.  Updates are grouped by target (each
+    // target subtracts its products in pivot order), so no two lanes write one word.
+    //   pivots of level l:        lvPiv[lvBeg[l] .. lvBeg[l+1])
+    //   multipliers of level l:   lsPos / lsPiv over lsBeg[l] .. lsBeg[l+1] (L position, pivot)
+    //   update targets of level l: tgPos over tgBeg[l] .. tgBeg[l+1]; target t subtracts
+    //                              A[tuL[u]] * A[tuU[u]] for u in tgUpd[t] .. tgUpd[t+1]
+    //   forward solve, level l:   rows fwRow over fwBeg[l] .. fwBeg[l+1]; row r subtracts
+    //                              A[flPos[e]] * x[flK[e]] for e in fwEnt[r] .. fwEnt[r+1]
+    //   backward solve, level l:  rows bwRow over bwBeg[l] .. bwBeg[l+1]; row r subtracts
+    //                              A[buPos[e]] * x[buK[e]] for e in bwEnt[r] .. bwEnt[r+1]
+    //                              (levels run last to first; x[k] of the level's pivots is
+    //                              scaled by the pivot reciprocal first)
+    int              nLevels = 0;
+    std::vector<int> lvBeg, lvPiv, lsBeg, lsPos, lsPiv, tgBeg, tgPos, tgUpd, tuL, tuU;
+    std::vector<int> fwBeg, fwRow, fwEnt, flPos, flK, bwBeg, bwRow, bwEnt, buPos, buK;
 };
 
 WarpPlan buildWarpPlan(const SparsePlan& P, const int* rbeg, const int* rspec, const int* rcnt, const int* pbeg,

@@ -82,9 +82,11 @@ enum nnet_solver
  * the dense solver always runs one thread per particle, like the reference's kernel). */
 enum nnet_layout
 {
-    NNET_LAYOUT_AUTO   = 0, /* library choice (currently: warp per particle) */
-    NNET_LAYOUT_THREAD = 1, /* one thread per particle, Newton system in strided global scratch */
-    NNET_LAYOUT_WARP   = 2, /* one warp per particle, Newton system in shared memory */
+    NNET_LAYOUT_AUTO    = 0, /* library choice (currently: batched warps) */
+    NNET_LAYOUT_THREAD  = 1, /* one thread per particle, Newton system in strided global scratch */
+    NNET_LAYOUT_WARP    = 2, /* one warp per particle, Newton system in shared memory */
+    NNET_LAYOUT_BATCHED = 3, /* 32 particles per warp in lockstep: per-particle scalar work one
+                                lane per particle, each Newton system by the whole warp */
 };
 
 typedef struct nnet_context* nnet_handle;

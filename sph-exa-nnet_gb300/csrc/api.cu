@@ -400,11 +400,21 @@ void nnet_gb300::Workspace::release()
     scratch = nullptr, counters = nullptr, doubles = 0;
 }
 
+int nnet_gb300::occupancy(const KernelInfo& ki, int& perSM)
+{
+    if (ki.smem > 48 * 1024)
+        NNET_CUDA(cudaFuncSetAttribute(ki.func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ki.smem));
+    NNET_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, ki.func, ki.block, ki.smem));
+    return NNET_SUCCESS;
+}
+
 KernelInfo nnet_gb300::burnKernel(nnet_context* h, int net, int eos, int solver)
 {
     if (solver == NNET_SOLVER_DENSE_FP64) return denseKernel(net, eos);
     const int mixed = solver == NNET_SOLVER_MIXED;
-    return h->layout == NNET_LAYOUT_THREAD ? sparseKernel(net, eos, mixed) : warpKernel(net, eos, mixed);
+    if (h->layout == NNET_LAYOUT_THREAD) return sparseKernel(net, eos, mixed);
+    if (h->layout == NNET_LAYOUT_WARP) return warpKernel(net, eos, mixed);
+    return batchKernel(net, eos, mixed);
 }
 
 size_t nnet_gb300::maxScratchDoubles(nnet_context* h, int solver)
@@ -416,7 +426,7 @@ size_t nnet_gb300::maxScratchDoubles(nnet_context* h, int solver)
             const KernelInfo ki = burnKernel(h, net, eos, solver);
             if (!ki.perSlot) continue;
             int perSM = 0;
-            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, ki.func, ki.block, 0) != cudaSuccess) perSM = 1;
+            if (occupancy(ki, perSM) != NNET_SUCCESS) perSM = 1;
             m = std::max(m, (size_t)h->numSMs * std::max(perSM, 1) * ki.block * ki.perSlot);
         }
     return m;
@@ -460,12 +470,10 @@ void fillParams(const nnet_burn_args* a, unsigned long long* counters, BurnParam
 int gridFor(nnet_context* h, const KernelInfo& ki, size_t P, size_t& blocks, size_t& slots)
 {
     int perSM = 0;
-    if (ki.smem > 48 * 1024)
-        NNET_CUDA(cudaFuncSetAttribute(ki.func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ki.smem));
-    NNET_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, ki.func, ki.block, ki.smem));
+    if (int rc = occupancy(ki, perSM)) return rc;
     if (perSM < 1) return fail(NNET_ERR_TOO_LARGE, "burn kernel does not fit on an SM");
     const size_t maxBlocks = (size_t)h->numSMs * perSM;
-    const size_t perBlock  = ki.smem ? ki.block / 32 : ki.block; // particles in flight per block
+    const size_t perBlock  = ki.block / ki.lanesPerParticle; // particles in flight per block
     const size_t need      = (P + perBlock - 1) / perBlock;
     blocks                 = need < maxBlocks ? need : maxBlocks;
     slots                  = blocks * ki.block;
@@ -505,7 +513,7 @@ int nnet_gb300::launchBurn(nnet_context* h, const nnet_burn_args* a, Workspace& 
 extern "C" int nnet_set_layout(nnet_handle h, int layout)
 {
     if (!h) return fail(NNET_ERR_INVALID, "null handle");
-    if (layout < NNET_LAYOUT_AUTO || layout > NNET_LAYOUT_WARP) return fail(NNET_ERR_INVALID, "unknown layout");
+    if (layout < NNET_LAYOUT_AUTO || layout > NNET_LAYOUT_BATCHED) return fail(NNET_ERR_INVALID, "unknown layout");
     h->layout = layout;
     return NNET_SUCCESS;
 }

@@ -1,0 +1,549 @@
+// Batched-warp forms of the sparse and mixed-precision burn: each warp carries 32
+// particles in lockstep, one per lane, through Newton iterations.
+//
+// A Newton iteration has two kinds of work.  The per-particle scalar part (temperature
+// checks, the Helmholtz EOS, the special CF88 rates, the Coulomb and fit-power factors,
+// electron captures, timestep control) is a few thousand FP64 instructions of branchy
+// scalar code; the system part (≈150 fitted rates, fluxes, Jacobian, sparse LU) is wide.
+// Here the scalar part runs SIMD across the warp's 32 particles (lane l = particle l), and
+// the system part runs warp-cooperatively on one particle at a time with the shared-memory
+// machinery of warp_system.cuh.  Per warp iteration:
+//   S1 (lanes)     pre-iteration checks; finished particles are released and replaced
+//   V1 (per slot)  apply the last decision to the slot's abundances (accept / continue),
+//                  write back a finished particle, load a new one, θ-blend, Σ Y and Σ Y Z
+//   S2 (lanes)     EOS and every temperature/density-only rate factor into the slot table
+//   V2 (per slot)  rates, fluxes, system, sparse LU solve, Newton candidate
+//   S3 (lanes)     acceptance, rejection and timestep control; release / replace
+// Abundances live in per-slot global scratch (contiguous per slot, L2-resident); the slot
+// table and one Newton system per warp live in shared memory.
+#include "launch.hpp"
+#include "warp_system.cuh"
+
+namespace nnet_gb300
+{
+
+namespace
+{
+
+// per-slot scalars, field-major in shared memory: field f of slot l at sc[f * 32 + l]
+enum SlotField : int
+{
+    fT, fTth, fRho, fDrho, fDt, fCv, fDpdT,
+    fGam, fGs, fGq, fGp, fGl, fNakbt, fCorr,
+    fT9, fT913, fT923, fT953, fT9i, fT9i2, fT9i13, fT9i23, fT9i43, fLt9,
+    fVal1, fVal2, fVal3, fVal4, fTwoT, fKb,
+    fSp0,             // 9 special rates (value, derivative), screened, in the network's slot order
+    fEv0 = fSp0 + 18, // net87: rate 309, d/dT, rate 310, d/dT, BE shift of n and p
+    kSlotFields = fEv0 + 6
+};
+
+// rate slots of the special rates, in the order they are stored
+__device__ __forceinline__ int specialSlot(int net, int k)
+{
+    if (net == 14)
+    {
+        constexpr int s14[9] = {0, 1, 2, 13, 14, 15, 16, 17, 18}; // e3a ecag eoag e2c eco e2o l3a lcag loag
+        return s14[k];
+    }
+    constexpr int s86[9] = {0, 1, 2, 3, 4, 5, 156, 157, 158}; // e2c eco e2o e3a ecag eoag l3a lcag loag
+    return s86[k];
+}
+
+enum : int
+{
+    ACT_ACCEPT = 1, // Y <- clipped candidate
+    ACT_CONT   = 2, // Yn <- clipped candidate
+    ACT_WRITE  = 4, // write the slot's Y back to the particle arrays (particle pw)
+    ACT_LOAD   = 8, // load a newly acquired particle's Y
+    ACT_BLEND  = 16 // θ-blend for the iteration about to run
+};
+
+template<int NET>
+constexpr int padN()
+{
+    return (NET + 3) & ~3;
+}
+
+// take the next particle of the queue for this lane (skipped ones are completed here)
+__device__ bool acquireLane(const BurnParams& bp, ParticleState& s)
+{
+    for (;;)
+    {
+        const unsigned long long q = atomicAdd(bp.queue, 1ull);
+        if (q >= bp.P) return false;
+        const size_t p     = bp.order ? (size_t)bp.order[q] : (size_t)q;
+        const int    phase = bp.rs.phase ? bp.rs.phase[p] : 0;
+        if (phase == 2) continue;
+        const double rho = bp.rho[p], T = bp.T[p];
+        if (phase == 0 && !(rho > k::minRho && T > k::minTemp))
+        {
+            if (bp.status) bp.status[p] = ST_SKIPPED;
+            if (bp.substeps) bp.substeps[p] = 0;
+            if (bp.iterations) bp.iterations[p] = 0;
+            atomicAdd(bp.stats + 2 + ST_SKIPPED, 1ull);
+            finishSegment(bp, p);
+            continue;
+        }
+        s.p = p, s.T = T, s.dt = bp.dt[p], s.rho = rho, s.i = 1;
+        if (phase == 1)
+        {
+            const ResumeState& r = bp.rs;
+            s.elapsed = r.elapsed[p], s.nextT = r.nextT[p], s.drho = r.drho[p], s.nit = r.nit[p];
+            s.nsub = r.nsub[p], s.cdDt = r.cdDt[p], s.cdNt = r.cdNt[p], s.cdPower = r.cdPower[p];
+            s.cdSteps = r.cdSteps[p];
+        }
+        else
+        {
+            double drho = 0;
+            if (bp.useDrhodt && bp.rhoM1 && bp.rhoM1[p] != 0) drho = (rho - bp.rhoM1[p]) / bp.previousDt;
+            s.elapsed = 0, s.nextT = 0, s.drho = drho, s.nit = 0, s.nsub = 0;
+            s.cycleReset();
+        }
+        s.nit0 = s.nit;
+        return true;
+    }
+}
+
+// scalar outputs of a finished (st >= 0) or paused (kPaused) particle; Y is written in V1
+__device__ void releaseLane(const BurnParams& bp, const ParticleState& s, int st)
+{
+    const size_t p = s.p;
+    bp.T[p]        = s.T;
+    bp.dt[p]       = s.dt;
+    atomicAdd(bp.stats + 0, (unsigned long long)(s.nit - s.nit0));
+    if (st == kPaused)
+    {
+        const ResumeState& r = bp.rs;
+        r.elapsed[p] = s.elapsed, r.nextT[p] = s.nextT, r.drho[p] = s.drho, r.nit[p] = s.nit, r.nsub[p] = s.nsub;
+        r.cdDt[p] = s.cdDt, r.cdNt[p] = s.cdNt, r.cdPower[p] = s.cdPower, r.cdSteps[p] = s.cdSteps;
+        r.phase[p] = 1;
+        return;
+    }
+    if (bp.status) bp.status[p] = st;
+    if (bp.substeps) bp.substeps[p] = s.nsub;
+    if (bp.iterations) bp.iterations[p] = (int32_t)s.nit;
+    atomicAdd(bp.stats + 1, (unsigned long long)s.nsub);
+    atomicAdd(bp.stats + 2 + st, 1ull);
+    finishSegment(bp, p);
+}
+
+// S2: everything of one Newton iteration that depends on (T, rho) of the slot only
+template<int NET, int EOS>
+__device__ void slotScalars(const NetView& nv, const HelmView& hv, double mu, double* sc, int lane, double T,
+                            double Tth, double rhoT, double drho, double dt, double abar, double zbar, double yElec)
+{
+    auto put = [&](int f, double v) { sc[f * 32 + lane] = v; };
+    EosResult eos;
+    if constexpr (EOS == NNET_EOS_IDEAL_GAS)
+        eos = idealGasEos(mu, Tth, rhoT);
+    else
+        eos = helmholtzEos(hv, abar, zbar, Tth, rhoT);
+    put(fT, T), put(fTth, Tth), put(fRho, rhoT), put(fDrho, drho), put(fDt, dt), put(fCv, eos.cv);
+    put(fDpdT, eos.dpdT);
+    const CoulombFast cf(Tth, rhoT);
+    put(fGam, cf.gam), put(fGs, cf.gs), put(fGq, cf.gq), put(fGp, cf.gp), put(fGl, cf.gl), put(fNakbt, cf.nakbt);
+    put(fCorr, cf.corr);
+    const FitT v(Tth);
+    put(fT9, v.t9), put(fT913, v.t913), put(fT923, v.t923), put(fT953, v.t953), put(fT9i, v.t9i);
+    put(fT9i2, v.t9i2), put(fT9i13, v.t9i13), put(fT9i23, v.t9i23), put(fT9i43, v.t9i43), put(fLt9, v.lt9);
+    if constexpr (NET == 14)
+    {
+        const double t9 = Tth / 1.e9, t9i = 1.e0 / t9, lt9 = log(t9);
+        const double val1 = 11.6045e0 * t9i;
+        put(fVal1, val1), put(fVal2, 1.5e0 * lt9), put(fVal3, val1 * t9i * 1e-9), put(fVal4, 1.5e-9 * t9i);
+    }
+    else
+    {
+        const double t9 = Tth * 1e-09, t9i = 1. / t9;
+        const double val1 = 11.6045 * t9i;
+        put(fVal1, val1), put(fVal2, 1.5 * log(t9)), put(fVal3, val1 * t9i * 1e-9), put(fVal4, 1.5e-9 * t9i);
+    }
+    put(fTwoT, 2. / Tth), put(fKb, (double)temperatureRange(Tth));
+    Special s;
+    specialRates(Tth, s);
+    auto m = [&](int i) { return (NET != 14 && i == 1) ? 0. : cf.mu(nv, i); }; // neutrons carry no screening
+    if constexpr (NET == 14)
+    {
+        const double m0 = m(0), m1 = m(1), m2 = m(2), m3 = m(3), m4 = m(4), m5 = m(5);
+        screenFast(s.e3a, s.de3a, m0 + m0 - m1 + m0, Tth);
+        screenFast(s.ecag, s.decag, m1 + m0 - m2, Tth);
+        screenFast(s.eoag, s.deoag, m2 + m0 - m3, Tth);
+        screenFast(s.e2c, s.de2c, 2. * m1 - m3, Tth);
+        screenFast(s.eco, s.deco, m1 + m2 - m4, Tth);
+        screenFast(s.e2o, s.de2o, 2. * m2 - m5, Tth);
+        const double o[18] = {s.e3a, s.de3a, s.ecag, s.decag, s.eoag, s.deoag, s.e2c, s.de2c, s.eco,
+                              s.deco, s.e2o, s.de2o, s.l3a, s.dl3a, s.lcag, s.dlcag, s.loag, s.dloag};
+        for (int k = 0; k < 18; ++k)
+            put(fSp0 + k, o[k]);
+    }
+    else
+    {
+        auto dmu = [&](int i) {
+            return m(__ldg(nv.mainReactant + i)) + m(__ldg(nv.secondaryReactant + i)) - m(__ldg(nv.mainProduct + i));
+        };
+        screenFast(s.e2c, s.de2c, dmu(0), Tth);
+        screenFast(s.eco, s.deco, dmu(1), Tth);
+        screenFast(s.e2o, s.de2o, dmu(2), Tth);
+        screenFast(s.e3a, s.de3a, dmu(4) + m(__ldg(nv.mainReactant + 4)), Tth);
+        screenFast(s.ecag, s.decag, dmu(5), Tth);
+        screenFast(s.eoag, s.deoag, dmu(6), Tth);
+        const double o[18] = {s.e2c, s.de2c, s.eco, s.deco, s.e2o, s.de2o, s.e3a, s.de3a, s.ecag,
+                              s.decag, s.eoag, s.deoag, s.l3a, s.dl3a, s.lcag, s.dlcag, s.loag, s.dloag};
+        for (int k = 0; k < 18; ++k)
+            put(fSp0 + k, o[k]);
+        if constexpr (NET == 87)
+        {
+            // electron captures (net87.hpp:117-175)
+            const double rhoElec = yElec * rhoT;
+            double       ev[12];
+            electronRates(nv, Tth, rhoElec, ev);
+            put(fEv0 + 0, rhoElec == 0 ? 0 : ev[0] / rhoElec), put(fEv0 + 1, rhoElec == 0 ? 0 : ev[1] / rhoElec);
+            put(fEv0 + 2, rhoElec == 0 ? 0 : ev[6] / rhoElec), put(fEv0 + 3, rhoElec == 0 ? 0 : ev[7] / rhoElec);
+            put(fEv0 + 4, -ev[3]), put(fEv0 + 5, -ev[9]);
+        }
+    }
+}
+
+// V2 rates of slot l from its table entries (same arithmetic as warpRates)
+template<int NET, bool MIXED>
+__device__ void slotRates(const NetView& nv, WarpSmem<NET, MIXED>& S, const double* c, int lane)
+{
+    auto g = [&](int f) { return c[f * 32]; };
+    CoulombFast cf;
+    cf.gam = g(fGam), cf.gs = g(fGs), cf.gq = g(fGq), cf.gp = g(fGp), cf.gl = g(fGl), cf.nakbt = g(fNakbt);
+    cf.corr = g(fCorr);
+    constexpr int NS = NET == 14 ? 14 : 86;
+    for (int i = lane; i < NS; i += 32)
+    {
+        S.BE[i] = cf.be(nv, i);
+        S.mu[i] = (NET != 14 && i == 1) ? 0. : cf.mu(nv, i);
+    }
+    __syncwarp();
+    FitT v;
+    v.t9 = g(fT9), v.t913 = g(fT913), v.t923 = g(fT923), v.t953 = g(fT953), v.t9i = g(fT9i), v.t9i2 = g(fT9i2);
+    v.t9i13 = g(fT9i13), v.t9i23 = g(fT9i23), v.t9i43 = g(fT9i43), v.lt9 = g(fLt9);
+    const double val1 = g(fVal1), val2 = g(fVal2), val3 = g(fVal3), val4 = g(fVal4), twoT = g(fTwoT);
+    const int    kb = (int)g(fKb);
+    if constexpr (NET == 14)
+    {
+        for (int i = 4 + lane; i < 14; i += 32)
+        {
+            const double* f  = nv.fit + (i - 4) * 8;
+            const double  f0 = __ldg(f), f1 = __ldg(f + 1), f2 = __ldg(f + 2), f3 = __ldg(f + 3),
+                         f4 = __ldg(f + 4), f5 = __ldg(f + 5), f6 = __ldg(f + 6), f7 = __ldg(f + 7);
+            const double coef  = f1 * v.t9i + f2 * v.t9i13 + f3 * v.t913 + f4 * v.t9 + f5 * v.t953 + f6 * v.lt9;
+            const double dcoef = (-f1 * v.t9i2 + (-f2 * v.t9i43 + f3 * v.t9i23 + 5 * f5 * v.t923) * (1. / 3.) + f4 +
+                                  f6 * v.t9i) *
+                                 1e-9;
+            const double q   = __ldg(nv.q + i - 4);
+            const double dmu = S.mu[i - 1] + S.mu[0] - S.mu[i];
+            const double e = exp(f0 + coef + dmu), de = e * (dcoef - dmu * twoT);
+            const double l = __ldg(nv.choose + (i - 4) * 24 + kb) / __ldg(nv.choose + (i + 1 - 4) * 24 + kb) *
+                             exp(coef + f7 - q * val1 + val2);
+            S.f[i - 1] = e, S.df[i - 1] = de;
+            S.f[16 + i - 1] = l, S.df[16 + i - 1] = l * (dcoef + q * val3 + val4);
+        }
+    }
+    else
+    {
+        for (int i = 7 + lane; i < 157; i += 32)
+        {
+            const double* f  = nv.fit + (i - 7) * 8;
+            const double  f0 = __ldg(f), f1 = __ldg(f + 1), f2 = __ldg(f + 2), f3 = __ldg(f + 3),
+                         f4 = __ldg(f + 4), f5 = __ldg(f + 5), f6 = __ldg(f + 6), f7 = __ldg(f + 7);
+            const double coef  = f1 * v.t9i + f2 * v.t9i13 + f3 * v.t913 + f4 * v.t9 + f5 * v.t953 + f6 * v.lt9;
+            const double dcoef = (-f1 * v.t9i2 + (-f2 * v.t9i43 + f3 * v.t9i23 + 5 * f5 * v.t923) * (1. / 3.) + f4 +
+                                  f6 * v.t9i) *
+                                 1e-9;
+            const int    mr = __ldg(nv.mainReactant + i), sr = __ldg(nv.secondaryReactant + i),
+                      mp = __ldg(nv.mainProduct + i);
+            const double part = __ldg(nv.choose + (mr - 5) * 24 + kb) / __ldg(nv.choose + (mp - 5) * 24 + kb);
+            const double q    = __ldg(nv.q + i - 7);
+            const double dmu  = S.mu[mr] + S.mu[sr] - S.mu[mp];
+            const double sdmu = i >= 137 ? dmu : 0.;
+            const double xr   = f7 + coef - val1 * q + (i < 137 ? val2 : 0.);
+            const double dr   = dcoef + val3 * q + (i < 137 ? val4 : 0.);
+            double       e, de, l, dl;
+            if ((i >= 137 && i < 154) || i == 156)
+            {
+                e = part * exp(xr + dmu), de = e * (dr - dmu * twoT);
+                l = exp(f0 + coef + sdmu), dl = l * (dcoef - sdmu * twoT);
+            }
+            else
+            {
+                e = exp(f0 + coef + dmu), de = e * (dcoef - dmu * twoT);
+                l = part * exp(xr + sdmu), dl = l * (dr - sdmu * twoT);
+            }
+            S.f[fwdSlot86(i)] = e, S.df[fwdSlot86(i)] = de;
+            S.f[revSlot86(i)] = l, S.df[revSlot86(i)] = dl;
+        }
+    }
+    if (lane < 9)
+    {
+        const int q = specialSlot(NET, lane);
+        S.f[q] = g(fSp0 + 2 * lane), S.df[q] = g(fSp0 + 2 * lane + 1);
+    }
+    if constexpr (NET == 87)
+    {
+        if (lane == 0)
+        {
+            S.BE[86] = __ldg(nv.BE + 86) + -1.5 * cf.nakbt;
+            S.BE[0]  = S.BE[0] + g(fEv0 + 4);
+            S.BE[1]  = S.BE[1] + g(fEv0 + 5);
+            S.f[309] = g(fEv0 + 0), S.df[309] = g(fEv0 + 1);
+            S.f[310] = g(fEv0 + 2), S.df[310] = g(fEv0 + 3);
+        }
+    }
+    __syncwarp();
+}
+
+} // namespace
+
+template<int NET, int EOS, bool MIXED>
+__global__ void __launch_bounds__(64, 1) burnBatchKernel(BurnParams bp, NetView nv, HelmView hv, double* scratch,
+                                                      size_t /*unused*/)
+{
+    using D                 = WDims<NET>;
+    constexpr int NP        = padN<NET>();
+    constexpr int VS        = 2 * NP; // per-slot abundances: Y (substep start), then Yn (iterate)
+    constexpr int perWarp   = WarpSmem<NET, MIXED>::doubles + kSlotFields * 32;
+    extern __shared__ __align__(16) double smem[];
+    const int             lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double*               wb   = smem + (size_t)warp * perWarp;
+    WarpSmem<NET, MIXED>  S(wb);
+    double*               sc   = wb + WarpSmem<NET, MIXED>::doubles;
+    const size_t          gw   = (size_t)blockIdx.x * (blockDim.x >> 5) + warp;
+    double*               vec0 = scratch + gw * 32 * VS; // slot l at vec0 + l * VS
+    const SparseView&     sp   = nv.sp;
+
+    // spread a small batch over every warp of the grid before filling warps
+    const size_t  warps  = (size_t)gridDim.x * (blockDim.x >> 5);
+    const size_t  first  = (bp.P + warps - 1) / warps;
+    ParticleState s;
+    bool          has = (size_t)lane < first && acquireLane(bp, s);
+    int           act = has ? ACT_LOAD : 0;
+    size_t        pw  = 0;
+    double        Tth = 0, rhoT = 0, used = 0, abar = 0, zbar = 0, yElec = 0, xT = 0;
+    bool          nanF = false;
+
+    for (;;)
+    {
+        // ---- S1: pre-iteration checks (newtonIteration prologue); finished ones are replaced
+        bool cont = false;
+        while (has)
+        {
+            int          st    = -1;
+            const double dtTot = bp.hydroDt;
+            if (s.nit >= bp.maxIter)
+                st = ST_MAXITER;
+            else if (bp.sliceIters > 0 && s.i == 1 && s.nit - s.nit0 >= bp.sliceIters)
+                st = kPaused;
+            else
+            {
+                rhoT = s.rho - s.drho * (dtTot - s.elapsed);
+                used = s.dt;
+                if (dtTot - s.elapsed < s.dt) used = dtTot - s.elapsed;
+                if (used == 0) st = ST_ZERO_DT;
+            }
+            if (st == -1)
+            {
+                ++s.nit;
+                const double guessT = s.i <= 1 ? s.T : s.nextT;
+                Tth                 = (1 - k::theta) * s.T + k::theta * guessT;
+                cont                = true;
+                break;
+            }
+            releaseLane(bp, s, st);
+            if (act & ACT_LOAD)
+                act &= ~ACT_LOAD; // never loaded: the particle arrays still hold its state
+            else
+                act |= ACT_WRITE, pw = s.p;
+            has = acquireLane(bp, s);
+            if (has) act |= ACT_LOAD;
+        }
+
+        // ---- V1: per slot, pending updates, write-back / load, θ-blend
+        const int a0 = act | (cont ? ACT_BLEND : 0);
+        for (unsigned m = __ballot_sync(kFull, a0 != 0); m; m &= m - 1)
+        {
+            const int    l  = __ffs(m) - 1;
+            const int    a  = __shfl_sync(kFull, a0, l);
+            const size_t po = __shfl_sync(kFull, (unsigned long long)pw, l);
+            const size_t pn = __shfl_sync(kFull, (unsigned long long)s.p, l);
+            const int    il = __shfl_sync(kFull, s.i, l);
+            double*      v  = vec0 + l * VS;
+            double*      vn = v + NP;
+            double       ab = 0, zb = 0, ynLast = 0;
+            for (int j = lane; j < D::N; j += 32)
+            {
+                double y = v[j], yn = vn[j];
+                if (a & ACT_ACCEPT) y = yn <= k::epsilonVector ? 0. : yn;
+                if (a & ACT_CONT) yn = yn <= k::epsilonVector ? 0. : yn;
+                if (a & ACT_WRITE) bp.Y[j][po] = y;
+                if (a & ACT_LOAD) y = bp.Y[j][pn];
+                if (a & ACT_BLEND)
+                {
+                    yn = (1 - k::theta) * y + k::theta * (il <= 1 ? y : yn);
+                    ab += yn, zb += yn * __ldg(nv.Z + j);
+                }
+                v[j] = y, vn[j] = yn, ynLast = yn;
+            }
+            if (a & ACT_BLEND)
+            {
+                ab = warpSum(ab), zb = warpSum(zb);
+                // net87: the blended electron abundance Y[86], last element of lane 86 % 32
+                const double ye = __shfl_sync(kFull, ynLast, 86 % 32);
+                if (lane == l) abar = ab, zbar = zb, yElec = NET == 87 ? ye : 0.;
+            }
+        }
+        act = 0;
+
+        // ---- S2: EOS and the (T, rho)-only rate factors of every running slot
+        if (cont) slotScalars<NET, EOS>(nv, hv, bp.mu, sc, lane, s.T, Tth, rhoT, s.drho, used, abar, zbar, yElec);
+        __syncwarp();
+
+        // ---- V2: per running slot, rates, system, solve, candidate
+        for (unsigned m = __ballot_sync(kFull, cont); m; m &= m - 1)
+        {
+            const int     l  = __ffs(m) - 1;
+            const double* c  = sc + l;
+            double*       v  = vec0 + l * VS;
+            double*       vn = v + NP;
+            for (int j = lane; j < D::N; j += 32)
+                S.Y[j] = v[j], S.Yn[j] = vn[j];
+            __syncwarp();
+            slotRates<NET, MIXED>(nv, S, c, lane);
+            warpAssemble<NET, MIXED>(nv, S, c[fT * 32], c[fTth * 32], c[fRho * 32], c[fDrho * 32], c[fCv * 32],
+                                     c[fDpdT * 32], c[fDt * 32], lane);
+            if constexpr (MIXED)
+            {
+                const int steps = warpSolveMixed<NET>(nv, S, c[fT * 32], lane, S.scale);
+                if (steps < 0)
+                {
+                    warpSolve64<NET, MIXED>(nv, S, lane); // not settled: this system is solved in FP64
+                    if (lane == 0) atomicAdd(bp.stats + 8, 1ull);
+                }
+                else if (steps && lane == 0)
+                    atomicAdd(bp.stats + 7, (unsigned long long)steps);
+            }
+            else
+                warpSolve64<NET, MIXED>(nv, S, lane);
+            bool nanl = false;
+            for (int j = lane; j < D::N; j += 32)
+            {
+                const double y = S.Y[j] + S.x[__ldg(sp.iperm + j + 1)];
+                vn[j]          = y;
+                nanl |= isnan(y);
+            }
+            const bool nan = __any_sync(kFull, nanl);
+            if (lane == l) nanF = nan, xT = S.x[sp.tNew];
+            __syncwarp();
+        }
+
+        // ---- S3: finalizeSystemSubstep / finalizeSystemNR (nuclear_net.hpp:724-782, :887-922)
+        if (cont)
+        {
+            const double dtTot  = bp.hydroDt;
+            double       usedDt = s.dt;
+            if (dtTot - s.elapsed < s.dt) usedDt = dtTot - s.elapsed;
+            const double lastT = s.nextT, T = s.T;
+            s.nextT            = T + xT;
+            int    iNext       = s.i;
+            bool   conv        = false;
+            double timestep    = 0;
+            if (nanF || isnan(s.nextT) || s.nextT < 0)
+            {
+                usedDt *= k::nanDtStep;
+                iNext = 0;
+            }
+            else
+            {
+                const double dT_T = fabs((s.nextT - T) / s.nextT);
+                if (s.i >= k::nrMinIt && dT_T > k::nrDTTarget * k::nrDTTol)
+                {
+                    usedDt *= k::nrDTTol / dT_T;
+                    iNext   = 0;
+                    s.nextT = T; // the candidate abundances are dropped (Y is kept)
+                }
+                else
+                {
+                    act                     = ACT_CONT; // clip the candidate
+                    const double correction = fabs((s.nextT - lastT) / s.nextT);
+                    if ((s.i >= k::nrMinIt && correction < k::nrItTol) || s.i >= k::nrMaxIt)
+                    {
+                        const double dTT = fabs((s.nextT - T) / s.nextT);
+                        timestep         = usedDt;
+                        usedDt           = (dTT == 0 ? k::maxDtStep : k::nrDTTarget / dTT) * timestep;
+                        usedDt           = fmin(usedDt, timestep * k::maxDtStep);
+                        usedDt           = fmax(usedDt, timestep * k::minDtStep);
+                        usedDt           = fmin(usedDt, k::nrMaxDt);
+                        conv             = true;
+                        act              = ACT_ACCEPT;
+                    }
+                }
+            }
+            if (dtTot - s.elapsed < s.dt)
+            {
+                if (usedDt < dtTot - s.elapsed) s.dt = usedDt;
+            }
+            else
+                s.dt = usedDt;
+            int st = -1;
+            if (conv)
+            {
+                s.T = s.nextT;
+                s.elapsed += timestep;
+                ++s.nsub;
+                s.i = 1;
+                if ((dtTot - s.elapsed) / dtTot < k::substepDtTol)
+                    st = ST_OK;
+                else
+                    s.cycleReset();
+            }
+            else if (iNext == 0)
+            {
+                if (s.cycleRejected())
+                    st = ST_LIVELOCK;
+                else
+                    s.i = 1;
+            }
+            else
+                s.i = iNext + 1;
+            if (st >= 0)
+            {
+                releaseLane(bp, s, st);
+                act |= ACT_WRITE, pw = s.p;
+                has = acquireLane(bp, s);
+                if (has) act |= ACT_LOAD;
+            }
+        }
+        if (!__any_sync(kFull, has || act != 0)) break;
+    }
+}
+
+namespace
+{
+template<int NET, int EOS, bool MIXED>
+KernelInfo batchInfo()
+{
+    constexpr size_t perWarp = WarpSmem<NET, MIXED>::doubles + kSlotFields * 32;
+    // lanesPerParticle = 32: a small batch is spread one particle per warp over the grid
+    return {(const void*)burnBatchKernel<NET, EOS, MIXED>, (size_t)2 * padN<NET>(), 64, WDims<NET>::NNZ,
+            2 * perWarp * sizeof(double), 32};
+}
+
+template<bool MIXED>
+KernelInfo pickBatch(int net, int eos)
+{
+    if (net == 14) return eos ? batchInfo<14, 1, MIXED>() : batchInfo<14, 0, MIXED>();
+    if (net == 86) return eos ? batchInfo<86, 1, MIXED>() : batchInfo<86, 0, MIXED>();
+    return eos ? batchInfo<87, 1, MIXED>() : batchInfo<87, 0, MIXED>();
+}
+} // namespace
+
+KernelInfo batchKernel(int net, int eos, int mixed)
+{
+    return mixed ? pickBatch<true>(net, eos) : pickBatch<false>(net, eos);
+}
+
+} // namespace nnet_gb300

@@ -8,64 +8,17 @@
 //   * accumulations are gathers in a fixed order (WarpPlan), and the few long lists (the
 //     p, n, alpha rows and columns) are split across the warp and summed with a fixed
 //     butterfly, so no two lanes write one word and results are deterministic;
-//   * the right-looking LU runs pivot by pivot: multipliers, then the pivot's independent
-//     updates in parallel; forward substitution by columns of L, backward by columns of U;
+//   * the right-looking LU runs by levels of mutually independent pivots: reciprocals,
+//     multipliers, then every target's updates in parallel; the solves follow the levels;
 //   * scalar work (EOS, special rates, Newton control) is evaluated identically by every
 //     lane, so control flow is warp-uniform.
 // The mixed form factors in FP32 (cheap reciprocals, FP32 pipe) with FP64 residuals; the
 // FP64 pipe, which bounds GB300 here, then only sees rates, assembly and residuals.
-#include "burn_policies.cuh"
 #include "launch.hpp"
-#include "sparse_plan.hpp"
+#include "warp_system.cuh"
 
 namespace nnet_gb300
 {
-
-constexpr unsigned kFull = 0xffffffffu;
-
-__device__ __forceinline__ double warpSum(double v)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1)
-        v += __shfl_xor_sync(kFull, v, o);
-    return v;
-}
-
-template<int NET>
-struct WDims
-{
-    static constexpr int N   = NET, n = NET + 1;
-    static constexpr int R   = NetDims<NET>::R;
-    static constexpr int NE  = NET == 14 ? 42 : NET == 86 ? 482 : 486; // reactant entries
-    static constexpr int NNZ = NET == 14 ? 104 : 1056;                 // factor capacity (checked on host)
-};
-
-// shared-memory layout of one warp (doubles; the float factor of the mixed form overlaps
-// the Jacobian bases `tr`, which are consumed before the solve)
-template<int NET, bool MIXED>
-struct WarpSmem
-{
-    using D = WDims<NET>;
-    static constexpr int oY = 0, oYn = oY + D::N, oF = oYn + D::N, oDF = oF + D::R, oBE = oDF + D::R,
-                         oA = oBE + D::N, oB = oA + D::NNZ, oDYdt = oB + D::n, oDYdT = oDYdt + D::N,
-                         oJdy = oDYdT + D::N, oTr = oJdy + D::N;
-    static constexpr int floatsD = (D::NNZ + 2 * D::n + 1) / 2;
-    static constexpr int doubles = oTr + (MIXED && floatsD > D::NE ? floatsD : D::NE);
-
-    static_assert(4 * D::n <= 2 * D::R + D::N, "solve vectors must fit the flux storage");
-    double *Y, *Yn, *f, *df, *BE, *A, *b, *dYdt, *mu, *dYdT, *jdy, *tr, *x, *r, *ipiv, *scale;
-    float * LU, *d, *ipiv32;
-
-    __device__ explicit WarpSmem(double* s)
-    {
-        Y = s + oY, Yn = s + oYn, f = s + oF, df = s + oDF, BE = s + oBE, A = s + oA, b = s + oB;
-        dYdt = s + oDYdt, dYdT = s + oDYdT, jdy = s + oJdy, tr = s + oTr;
-        mu = dYdt; // screening potentials live until the rates are done
-        // the solve vectors reuse the flux / binding-energy storage, dead after assembly
-        x = f, r = f + D::n, ipiv = f + 2 * D::n, scale = f + 3 * D::n;
-        LU = reinterpret_cast<float*>(tr), d = LU + D::NNZ, ipiv32 = d + D::n;
-    }
-};
 
 // ------------------------------------------------------------------ rates (warp)
 template<int NET, bool MIXED>
@@ -194,293 +147,6 @@ __device__ void warpRates(const NetView& nv, WarpSmem<NET, MIXED>& S, double T, 
         }
     }
     __syncwarp();
-}
-
-// ------------------------------------------------------------------ assembly (warp)
-template<int NET, bool MIXED>
-__device__ void warpAssemble(const NetView& nv, WarpSmem<NET, MIXED>& S, double T, double Tg, double rho,
-                             double drho_dt, double cv, double dpdT, double dt, int lane)
-{
-    using D                = WDims<NET>;
-    const SparseView& sp   = nv.sp;
-    const WarpView&   wv   = nv.wv;
-    // per-reaction fluxes (dY/dt terms, nuclear_net.hpp:347-381) and Jacobian bases
-    // (:395-438), in place of the rates
-    for (int q = lane; q < D::R; q += 32)
-    {
-        const int rb = __ldg(nv.rbeg + q), re = __ldg(nv.rbeg + q + 1);
-        double    f = S.f[q], df = S.df[q], base = f;
-        for (int k = rb; k < re; ++k)
-        {
-            const int    cnt = __ldg(nv.rcnt + k);
-            const double yr  = S.Yn[__ldg(nv.rspec + k)] * rho;
-            if (cnt != 1)
-            {
-                const double fac = cnt == 2 ? 2. : 6.;
-                f /= fac, df /= fac, base /= fac;
-            }
-            const double pw = ipowS(yr, cnt);
-            f *= pw, df *= pw, base *= ipowS(yr, cnt - 1);
-        }
-        S.f[q] = f / rho, S.df[q] = df / rho;
-        for (int k = rb; k < re; ++k)
-        {
-            const int id = __ldg(nv.rspec + k);
-            double    tr = base;
-            for (int o = rb; o < re; ++o)
-            {
-                const int os = __ldg(nv.rspec + o);
-                if (os != id) tr *= S.Yn[os] * rho;
-            }
-            S.tr[k] = base > k::epsilonSystem ? tr : 0.;
-        }
-    }
-    for (int p = lane; p < sp.nnz; p += 32)
-        S.A[p] = 0.;
-    __syncwarp();
-    // dY/dt and d(dY/dt)/dT per species
-    for (int s = lane; s < D::N; s += 32)
-    {
-        const int b0 = __ldg(wv.sgBeg + s), b1 = __ldg(wv.sgBeg + s + 1);
-        if (b1 - b0 > WarpPlan::kHeavy) continue;
-        double a = 0, c = 0;
-        for (int k = b0; k < b1; ++k)
-        {
-            const double w = __ldg(wv.sgCoef + k);
-            const int    r = __ldg(wv.sgRx + k);
-            a += w * S.f[r], c += w * S.df[r];
-        }
-        S.dYdt[s] = a, S.dYdT[s] = c;
-    }
-    for (int h = 0; h < wv.nSgHeavy; ++h)
-    {
-        const int s = __ldg(wv.sgHeavy + h), b0 = __ldg(wv.sgBeg + s), b1 = __ldg(wv.sgBeg + s + 1);
-        double    a = 0, c = 0;
-        for (int k = b0 + lane; k < b1; k += 32)
-        {
-            const double w = __ldg(wv.sgCoef + k);
-            const int    r = __ldg(wv.sgRx + k);
-            a += w * S.f[r], c += w * S.df[r];
-        }
-        a = warpSum(a), c = warpSum(c);
-        if (lane == 0) S.dYdt[s] = a, S.dYdT[s] = c;
-    }
-    // Jacobian entries
-    for (int m = lane; m < wv.nJ; m += 32)
-    {
-        const int b0 = __ldg(wv.jgBeg + m), b1 = __ldg(wv.jgBeg + m + 1);
-        if (b1 - b0 > WarpPlan::kHeavy) continue;
-        double a = 0;
-        for (int k = b0; k < b1; ++k)
-            a += __ldg(wv.jgCoef + k) * S.tr[__ldg(wv.jgEnt + k)];
-        S.A[__ldg(wv.jPos + m)] = a;
-    }
-    for (int h = 0; h < wv.nJgHeavy; ++h)
-    {
-        const int m = __ldg(wv.jgHeavy + h), b0 = __ldg(wv.jgBeg + m), b1 = __ldg(wv.jgBeg + m + 1);
-        double    a = 0;
-        for (int k = b0 + lane; k < b1; k += 32)
-            a += __ldg(wv.jgCoef + k) * S.tr[__ldg(wv.jgEnt + k)];
-        a = warpSum(a);
-        if (lane == 0) S.A[__ldg(wv.jPos + m)] = a;
-    }
-    __syncwarp();
-    // J (Yg - Y) per species row (nuclear_net.hpp:580-589)
-    for (int i = lane; i < D::N; i += 32)
-    {
-        const int b0 = __ldg(wv.rjBeg + i), b1 = __ldg(wv.rjBeg + i + 1);
-        if (b1 - b0 > WarpPlan::kHeavy) continue;
-        double a = 0;
-        for (int k = b0; k < b1; ++k)
-        {
-            const int m = __ldg(wv.rjEnt + k), j = __ldg(wv.jCol + m);
-            a += S.A[__ldg(wv.jPos + m)] * (S.Yn[j] - S.Y[j]);
-        }
-        S.jdy[i] = a;
-    }
-    for (int h = 0; h < wv.nRjHeavy; ++h)
-    {
-        const int i = __ldg(wv.rjHeavy + h), b0 = __ldg(wv.rjBeg + i), b1 = __ldg(wv.rjBeg + i + 1);
-        double    a = 0;
-        for (int k = b0 + lane; k < b1; k += 32)
-        {
-            const int m = __ldg(wv.rjEnt + k), j = __ldg(wv.jCol + m);
-            a += S.A[__ldg(wv.jPos + m)] * (S.Yn[j] - S.Y[j]);
-        }
-        a = warpSum(a);
-        if (lane == 0) S.jdy[i] = a;
-    }
-    __syncwarp();
-    // I - theta dt J, the temperature row / column and the right-hand side (:590-608)
-    const double mtd = -k::theta * dt;
-    for (int e = lane; e < sp.nsb; e += 32)
-    {
-        const int p = __ldg(sp.sbPos + e);
-        S.A[p]      = __ldg(sp.sbDiag + e) ? 1. - k::theta * dt * S.A[p] : mtd * S.A[p];
-    }
-    for (int i = lane; i < D::N; i += 32)
-    {
-        const double c0 = S.dYdT[i];
-        double       rh = S.dYdt[i] * dt;
-        rh              = rh + mtd * c0 * (Tg - T);
-        rh              = rh + mtd * S.jdy[i];
-        S.b[__ldg(sp.iperm + i + 1)] = rh;
-        S.A[__ldg(sp.col0Pos + i)]   = c0 * mtd;
-        S.A[__ldg(sp.row0Pos + i)]   = -S.BE[i] / cv;
-    }
-    if (lane == 0)
-    {
-        const double drho = drho_dt * dt, value1 = dpdT * drho / (rho * rho);
-        S.b[sp.tNew]  = T * value1 / cv;
-        S.A[sp.pos00] = 1 - k::theta * value1 / cv;
-    }
-    __syncwarp();
-}
-
-// ------------------------------------------------------------------ solves (warp)
-// Level-scheduled right-looking LU without pivoting, in place (FP64 or FP32): per level,
-// the pivots' reciprocals, then their multipliers, then every target's updates in pivot order.
-__device__ __forceinline__ double recip(double a) { return __drcp_rn(a); }
-__device__ __forceinline__ float  recip(float a) { return __frcp_rn(a); }
-
-template<typename F>
-__device__ void levelFactor(const SparseView& sp, const WarpView& wv, F* A, F* ipiv, int lane)
-{
-    for (int l = 0; l < wv.nLevels; ++l)
-    {
-        for (int q = __ldg(wv.lvBeg + l) + lane; q < __ldg(wv.lvBeg + l + 1); q += 32)
-        {
-            const int k = __ldg(wv.lvPiv + q);
-            ipiv[k]     = recip(A[__ldg(sp.kPiv + k)]);
-        }
-        __syncwarp();
-        for (int e = __ldg(wv.lsBeg + l) + lane; e < __ldg(wv.lsBeg + l + 1); e += 32)
-            A[__ldg(wv.lsPos + e)] *= ipiv[__ldg(wv.lsPiv + e)];
-        __syncwarp();
-        for (int t = __ldg(wv.tgBeg + l) + lane; t < __ldg(wv.tgBeg + l + 1); t += 32)
-        {
-            const int pos = __ldg(wv.tgPos + t);
-            F         a   = A[pos];
-            for (int u = __ldg(wv.tgUpd + t), ue = __ldg(wv.tgUpd + t + 1); u < ue; ++u)
-                a = a - A[__ldg(wv.tuL + u)] * A[__ldg(wv.tuU + u)];
-            A[pos] = a;
-        }
-        __syncwarp();
-    }
-}
-
-// x <- U^-1 L^-1 x with the factor of levelFactor (same level schedule)
-template<typename F>
-__device__ void levelSolve(const WarpView& wv, const F* A, const F* ipiv, F* x, int lane)
-{
-    for (int l = 0; l < wv.nLevels; ++l)
-    {
-        for (int r = __ldg(wv.fwBeg + l) + lane; r < __ldg(wv.fwBeg + l + 1); r += 32)
-        {
-            const int row = __ldg(wv.fwRow + r);
-            F         a   = x[row];
-            for (int e = __ldg(wv.fwEnt + r), ee = __ldg(wv.fwEnt + r + 1); e < ee; ++e)
-                a = a - A[__ldg(wv.flPos + e)] * x[__ldg(wv.flK + e)];
-            x[row] = a;
-        }
-        __syncwarp();
-    }
-    for (int li = 0; li < wv.nLevels; ++li)
-    {
-        const int l = wv.nLevels - 1 - li;
-        for (int q = __ldg(wv.lvBeg + l) + lane; q < __ldg(wv.lvBeg + l + 1); q += 32)
-        {
-            const int k = __ldg(wv.lvPiv + q);
-            x[k]        = x[k] * ipiv[k];
-        }
-        __syncwarp();
-        for (int r = __ldg(wv.bwBeg + li) + lane; r < __ldg(wv.bwBeg + li + 1); r += 32)
-        {
-            const int row = __ldg(wv.bwRow + r);
-            F         a   = x[row];
-            for (int e = __ldg(wv.bwEnt + r), ee = __ldg(wv.bwEnt + r + 1); e < ee; ++e)
-                a = a - A[__ldg(wv.buPos + e)] * x[__ldg(wv.buK + e)];
-            x[row] = a;
-        }
-        __syncwarp();
-    }
-}
-
-// FP64: factor A in place, x = A^-1 b
-template<int NET, bool MIXED>
-__device__ void warpSolve64(const NetView& nv, WarpSmem<NET, MIXED>& S, int lane)
-{
-    levelFactor<double>(nv.sp, nv.wv, S.A, S.ipiv, lane);
-    for (int i = lane; i < WDims<NET>::n; i += 32)
-        S.x[i] = S.b[i];
-    __syncwarp();
-    levelSolve<double>(nv.wv, S.A, S.ipiv, S.x, lane);
-}
-
-// rows scaled by powers of two, FP32 factorisation, FP64 residual refinement; returns
-// the refinement steps, or -1 if the corrections did not settle (caller re-solves in FP64)
-template<int NET>
-__device__ int warpSolveMixed(const NetView& nv, WarpSmem<NET, true>& S, double T, int lane, double* scale)
-{
-    using D              = WDims<NET>;
-    const SparseView& sp = nv.sp;
-    const WarpView&   wv = nv.wv;
-    // row scales from the exponent bits (integer work), then the FP32 copy
-    for (int i = lane; i < D::n; i += 32)
-    {
-        int e = 0;
-        for (int p = __ldg(sp.rowBeg + i), pe = __ldg(sp.rowBeg + i + 1); p < pe; ++p)
-            e = max(e, (int)((__double_as_longlong(S.A[p]) >> 52) & 0x7ff));
-        scale[i] = e == 0 ? 1. : ldexp(1., 1023 - e); // 2^-ilogb(max |a_ij|)
-    }
-    __syncwarp();
-    for (int p = lane; p < sp.nnz; p += 32)
-        S.LU[p] = (float)(S.A[p] * scale[__ldg(sp.posRow + p)]);
-    __syncwarp();
-    levelFactor<float>(sp, wv, S.LU, S.ipiv32, lane);
-    for (int i = lane; i < D::n; i += 32)
-        S.x[i] = 0., S.r[i] = S.b[i];
-    __syncwarp();
-    for (int steps = 0;; ++steps)
-    {
-        for (int i = lane; i < D::n; i += 32)
-            S.d[i] = (float)(S.r[i] * scale[i]);
-        __syncwarp();
-        levelSolve<float>(wv, S.LU, S.ipiv32, S.d, lane);
-        bool conv = true;
-        for (int i = lane; i < D::n; i += 32)
-        {
-            const double di = (double)S.d[i], xi = S.x[i] + di;
-            const int    o  = __ldg(sp.perm + i);
-            const double sc = o == 0 ? T : fabs(S.Y[o - 1]);
-            conv &= fabs(di) <= kRefineTol * (fabs(xi) + sc) && isfinite(xi); // an FP32 overflow is not convergence
-            S.x[i] = xi;
-        }
-        conv = __all_sync(kFull, conv);
-        __syncwarp();
-        if (conv) return steps;
-        if (steps == kMaxRefine) return -1;
-        // r = b - A x (FP64, rows over lanes; the long rows split across the warp)
-        for (int i = lane; i < D::n; i += 32)
-        {
-            const int p0 = __ldg(sp.rowBeg + i), p1 = __ldg(sp.rowBeg + i + 1);
-            if (p1 - p0 > WarpPlan::kHeavy) continue;
-            double s = S.b[i];
-            for (int p = p0; p < p1; ++p)
-                s -= S.A[p] * S.x[__ldg(sp.posCol + p)];
-            S.r[i] = s;
-        }
-        for (int h = 0; h < wv.nRowHeavy; ++h)
-        {
-            const int i = __ldg(wv.rowHeavy + h), p0 = __ldg(sp.rowBeg + i), p1 = __ldg(sp.rowBeg + i + 1);
-            double    s = 0;
-            for (int p = p0 + lane; p < p1; p += 32)
-                s += S.A[p] * S.x[__ldg(sp.posCol + p)];
-            s = warpSum(s);
-            if (lane == 0) S.r[i] = S.b[i] - s;
-        }
-        __syncwarp();
-    }
 }
 
 // ------------------------------------------------------------------ driver (warp)
@@ -718,7 +384,7 @@ template<int NET, int EOS, bool MIXED>
 static KernelInfo warpInfo()
 {
     return {(const void*)burnWarpKernel<NET, EOS, MIXED>, 0, 128, WDims<NET>::NNZ,
-            4 * WarpSmem<NET, MIXED>::doubles * sizeof(double)};
+            4 * WarpSmem<NET, MIXED>::doubles * sizeof(double), 32};
 }
 
 template<bool MIXED>

@@ -35,6 +35,9 @@ struct Workspace
 int launchBurn(struct ::nnet_context* h, const nnet_burn_args* args, Workspace& ws, cudaStream_t st,
                const ResumeState* rs, long long sliceIters, unsigned long long* segFinished);
 
+// resident blocks per SM of a burn kernel (sets its dynamic shared-memory limit first)
+int occupancy(const KernelInfo& ki, int& perSM);
+
 // kernel of (network, eos, solver) under the context's layout
 KernelInfo burnKernel(struct ::nnet_context* h, int net, int eos, int solver);
 

@@ -12,11 +12,13 @@ struct KernelInfo
     size_t      perSlot;   // scratch doubles per thread slot
     int         block;     // threads per block
     int         maxNnz;    // sparse forms: capacity of the factor storage (0 = dense)
-    size_t      smem = 0;  // warp-per-particle forms: dynamic shared memory per block (bytes)
+    size_t      smem = 0;  // warp-cooperative forms: dynamic shared memory per block (bytes)
+    int         lanesPerParticle = 1; // 32: one warp per particle in flight
 };
 
 KernelInfo denseKernel(int net, int eos);
 KernelInfo sparseKernel(int net, int eos, int mixed);
-KernelInfo warpKernel(int net, int eos, int mixed); // one warp per particle (smem != 0)
+KernelInfo warpKernel(int net, int eos, int mixed);  // one warp per particle
+KernelInfo batchKernel(int net, int eos, int mixed); // 32 particles per warp in lockstep
 
 } // namespace nnet_gb300

@@ -323,6 +323,7 @@ __device__ __forceinline__ double screeningGamma(double T, double rho)
 struct FitT
 {
     double t9, t913, t923, t953, t9i, t9i2, t9i13, t9i23, t9i43, lt9;
+    FitT() = default; // fields filled by the caller (values computed elsewhere)
     __device__ explicit FitT(double T)
     {
         t9 = T / 1.e9, t913 = pow(t9, 1. / 3.), t923 = t913 * t913, t953 = pow(t9, 5. / 3.);

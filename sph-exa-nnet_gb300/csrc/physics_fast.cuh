@@ -21,6 +21,7 @@ namespace nnet_gb300
 struct CoulombFast
 {
     double gam, gs, gq, gp, gl, nakbt, corr;
+    CoulombFast() = default; // fields filled by the caller (values computed elsewhere)
     __device__ CoulombFast(double T, double rho)
     {
         const double kbt = NNET_KB * T;

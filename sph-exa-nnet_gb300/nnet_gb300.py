@@ -28,8 +28,8 @@ HELM_TABLE_PATH = os.path.join(HERE, "data", "helm_table.bin")
 NET14, NET86, NET87 = 14, 86, 87
 EOS_IDEAL_GAS, EOS_HELMHOLTZ = 0, 1
 SOLVER_DENSE_FP64, SOLVER_SPARSE_FP64, SOLVER_MIXED = 0, 1, 2
-LAYOUT_AUTO, LAYOUT_THREAD, LAYOUT_WARP = 0, 1, 2
-LAYOUTS = {"auto": LAYOUT_AUTO, "thread": LAYOUT_THREAD, "warp": LAYOUT_WARP}
+LAYOUT_AUTO, LAYOUT_THREAD, LAYOUT_WARP, LAYOUT_BATCHED = 0, 1, 2, 3
+LAYOUTS = {"auto": LAYOUT_AUTO, "thread": LAYOUT_THREAD, "warp": LAYOUT_WARP, "batched": LAYOUT_BATCHED}
 STATUS_NAMES = ["OK", "SKIPPED", "LIVELOCK", "MAXITER", "ZERO_DT"]
 NUM_REACTIONS = {14: 29, 86: 309, 87: 311}
 SOLVERS = {"dense": SOLVER_DENSE_FP64, "plain": SOLVER_DENSE_FP64, "sparse": SOLVER_SPARSE_FP64,
@@ -116,7 +116,7 @@ class Context:
             self.load_helmholtz_table(helmholtz_table)
 
     def set_layout(self, layout):
-        """Particle layout of the sparse / mixed solvers: "auto", "thread" or "warp"."""
+        """Particle layout of the sparse / mixed solvers: "auto", "thread", "warp" or "batched"."""
         _check(_lib.nnet_set_layout(self.handle, LAYOUTS[layout] if isinstance(layout, str) else int(layout)))
 
     def close(self):

@@ -119,13 +119,44 @@ def test_thread_layout_parity(ctx, port, name, P, solver):
     check(w, g, o)
 
 
-def test_warp_layout_deterministic(ctx):
-    """Two runs of the warp layout give bit-identical results (fixed-order gathers)."""
+@pytest.mark.parametrize("solver", ["sparse", "mixed"])
+@pytest.mark.parametrize("name,P", [("c1", 2048), ("c2", 256), ("c4", 128)])
+def test_warp_layout_parity(ctx, port, name, P, solver):
+    """The warp-per-particle layout of the sparse forms against the oracle."""
+    w = workloads.make(name, P=P, seed=3000 + P)
+    g = gpu_burn(ctx, w, solver, layout="warp")
+    ctx.set_layout("auto")
+    o = port.burn(w["net"], w["Y"], w["T"], w["rho"], w["dt"], w["hydro_dt"], w["eos"], w["mu"], max_iter=20000)
+    check(w, g, o)
+
+
+@pytest.mark.parametrize("layout", ["warp", "batched"])
+def test_warp_layouts_deterministic(ctx, layout):
+    """Two runs of a warp-cooperative layout give bit-identical results (fixed-order gathers
+    and reductions, no atomics on values)."""
     w = workloads.make("c2", P=512, seed=3)
-    a = gpu_burn(ctx, w, "sparse", layout="warp")
-    b = gpu_burn(ctx, w, "sparse", layout="warp")
+    a = gpu_burn(ctx, w, "sparse", layout=layout)
+    b = gpu_burn(ctx, w, "sparse", layout=layout)
+    ctx.set_layout("auto")
     for x, y in zip(a, b):
         assert np.array_equal(x, y)
+
+
+def test_batched_large_c1(ctx, port):
+    """More particles than the batched grid holds at once (the queue refills slots)."""
+    w = workloads.make("c1", P=40000, seed=41)
+    g = gpu_burn(ctx, w, "sparse", layout="batched")
+    o = port.burn(w["net"], w["Y"], w["T"], w["rho"], w["dt"], w["hydro_dt"], w["eos"], w["mu"], max_iter=20000)
+    check(w, g, o)
+
+
+def test_batched_small_and_ragged(ctx, port):
+    """Batches smaller than a warp and not a multiple of 32."""
+    for P in (1, 33, 100):
+        w = workloads.make("c2", P=P, seed=50 + P)
+        g = gpu_burn(ctx, w, "sparse", layout="batched")
+        o = port.burn(w["net"], w["Y"], w["T"], w["rho"], w["dt"], w["hydro_dt"], w["eos"], w["mu"], max_iter=20000)
+        check(w, g, o, min_frac=0.9 if P > 10 else 0.0)
 
 
 @pytest.mark.parametrize("solver", ["dense", "sparse", "mixed"])

@@ -218,6 +218,17 @@ int nnet_solver_info(int network, int solver, long long* factor_fma, long long* 
  * with a dependency-free probe kernel (no reference counterpart; roofline denominator). */
 int nnet_measure_fp64_peak(int device, double* tflops);
 
+/* nnet_burn for callers that cannot allocate device memory during a time step (codes whose
+ * device memory all belongs to their own arena allocator, or that cannot afford the device-wide
+ * synchronisation a cudaMalloc may cause).  No counterpart in the reference.  Same arguments
+ * and results as nnet_burn with the batched layout; sparse and mixed solvers only.  Allocates
+ * nothing: its slot scratch (5.5 MiB, 4096 particle slots) and counters are fixed arrays that
+ * every GPU loading the library holds until exit; the grid is capped to them, so any number of
+ * particles is accepted.  The first call on a device looks the arrays up (make it before any
+ * stream capture).  Calls share the arrays: calls that overlap on the GPU race, and
+ * nnet_get_stats does not report these calls. */
+int nnet_burn_noalloc(nnet_handle h, const nnet_burn_args* args, void* stream);
+
 /* Select the particle layout of the sparse and mixed solvers for later nnet_burn calls on
  * `h` (nnet_layout; no reference counterpart: chosen by the autotuner). */
 int nnet_set_layout(nnet_handle h, int layout);

@@ -510,6 +510,14 @@ int nnet_gb300::launchBurn(nnet_context* h, const nnet_burn_args* a, Workspace& 
     return NNET_SUCCESS;
 }
 
+// shared with the other translation units of the C ABI
+int nnet_gb300::validateBurn(nnet_context* h, const nnet_burn_args* a) { return validate(h, a); }
+void nnet_gb300::fillBurnParams(const nnet_burn_args* a, unsigned long long* counters, BurnParams& bp)
+{
+    fillParams(a, counters, bp);
+}
+int nnet_gb300::setError(int code, const char* msg) { return fail(code, msg); }
+
 extern "C" int nnet_set_layout(nnet_handle h, int layout)
 {
     if (!h) return fail(NNET_ERR_INVALID, "null handle");

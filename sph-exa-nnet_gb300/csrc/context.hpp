@@ -35,6 +35,11 @@ struct Workspace
 int launchBurn(struct ::nnet_context* h, const nnet_burn_args* args, Workspace& ws, cudaStream_t st,
                const ResumeState* rs, long long sliceIters, unsigned long long* segFinished);
 
+// argument checks and kernel parameters of nnet_burn; last-error message of the C ABI
+int  validateBurn(struct ::nnet_context* h, const nnet_burn_args* a);
+void fillBurnParams(const nnet_burn_args* a, unsigned long long* counters, BurnParams& bp);
+int  setError(int code, const char* msg);
+
 // resident blocks per SM of a burn kernel (sets its dynamic shared-memory limit first)
 int occupancy(const KernelInfo& ki, int& perSM);
 

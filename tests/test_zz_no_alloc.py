@@ -1,0 +1,98 @@
+"""nnet_burn_noalloc: the burn for callers that cannot allocate device memory mid-step (codes
+whose device memory all belongs to their own arena allocator, or that cannot afford the
+device-wide synchronisation a cudaMalloc may cause).  Called here through the C ABI with
+ctypes and compared with nnet_burn (the batched layout) on the same inputs, twice in a row,
+because the fixed scratch array keeps the previous call's contents.  The workload holds more
+particles than the array has slots, so slots are refilled from the work queue.
+
+This file sorts last so that a run stopping at its first failure has run every other test."""
+import ctypes
+
+import pytest
+
+import workloads
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import torch
+    import nnet_gb300 as nn
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    c = nn.Context(0)
+    yield c
+    c.close()
+
+
+def _args(nn, w, Y, T, rho, dt, st, solver, max_iter):
+    rows = [Y[j] for j in range(w["net"])]
+    yp = (ctypes.c_void_p * w["net"])(*[r.data_ptr() for r in rows])
+    eos = nn.EOS_IDEAL_GAS if w["eos"].startswith("ideal") else nn.EOS_HELMHOLTZ
+    a = nn._BurnArgs(network=w["net"], eos=eos, ideal_gas_mu=w["mu"], solver=nn.SOLVERS[solver],
+                     num_particles=T.numel(), Y=ctypes.cast(yp, ctypes.POINTER(ctypes.c_void_p)),
+                     T=T.data_ptr(), rho=rho.data_ptr(), rho_m1=None, dt=dt.data_ptr(), hydro_dt=w["hydro_dt"],
+                     previous_dt=0.0, use_drhodt=0, max_newton_iterations=max_iter, status=st.data_ptr(),
+                     substeps=None, iterations=None)
+    return a, yp
+
+
+def _inputs(w):
+    import torch
+    dev = torch.device("cuda:0")
+    P = w["T"].size
+    return (torch.tensor(w["Y"], device=dev), torch.tensor(w["T"], device=dev), torch.tensor(w["rho"], device=dev),
+            torch.tensor(w["dt"], device=dev), torch.full((P,), -1, dtype=torch.int32, device=dev))
+
+
+def _lib():
+    import nnet_gb300 as nn
+    lib = nn.load_library()
+    lib.nnet_burn_noalloc.argtypes = [ctypes.c_void_p, ctypes.POINTER(nn._BurnArgs), ctypes.c_void_p]
+    return lib
+
+
+def _noalloc(ctx, w, solver, max_iter=20000):
+    import torch
+    import nnet_gb300 as nn
+    lib = _lib()
+    Y, T, rho, dt, st = _inputs(w)
+    a, keep = _args(nn, w, Y, T, rho, dt, st, solver, max_iter)
+    s = torch.cuda.current_stream(0)
+    rc = lib.nnet_burn_noalloc(ctx.handle, ctypes.byref(a), ctypes.c_void_p(s.cuda_stream))
+    assert rc == 0, lib.nnet_last_error_message().decode()
+    torch.cuda.synchronize()
+    return Y.cpu().numpy(), T.cpu().numpy(), dt.cpu().numpy(), st.cpu().numpy()
+
+
+def _existing(ctx, w, solver, max_iter=20000):
+    import torch
+    Y, T, rho, dt, st = _inputs(w)
+    ctx.set_layout("batched")
+    ctx.burn(w["net"], Y, T, rho, dt, w["hydro_dt"], eos=w["eos"], mu=w["mu"], solver=solver, status=st,
+             max_iter=max_iter)
+    ctx.set_layout("auto")
+    torch.cuda.synchronize()
+    return Y.cpu().numpy(), T.cpu().numpy(), dt.cpu().numpy(), st.cpu().numpy()
+
+
+@pytest.mark.parametrize("solver", ["sparse", "mixed"])
+def test_noalloc_matches_nnet_burn_twice(ctx, solver):
+    from test_gpu_parity import check
+    w = workloads.make("c2", P=6000, seed=606)  # more particles than the 4096 fixed slots
+    ref = _existing(ctx, w, solver)
+    for _ in range(2):
+        check(w, _noalloc(ctx, w, solver), ref)  # the parity tests' tolerance
+
+
+def test_noalloc_small_and_rejects_dense(ctx):
+    import nnet_gb300 as nn
+    from test_gpu_parity import check
+    w = workloads.make("c1", P=40, seed=7)
+    check(w, _noalloc(ctx, w, "sparse"), _existing(ctx, w, "sparse"), min_frac=0.9)
+    lib = _lib()
+    Y, T, rho, dt, st = _inputs(w)
+    a, keep = _args(nn, w, Y, T, rho, dt, st, "dense", 100)
+    assert lib.nnet_burn_noalloc(ctx.handle, ctypes.byref(a), None) == -1  # NNET_ERR_INVALID
+    assert b"sparse and mixed" in lib.nnet_last_error_message()

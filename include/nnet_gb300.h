@@ -144,8 +144,9 @@ int nnet_load_helmholtz_table_file(nnet_handle h, const char* path);
  * nnet_get_stats after the stream has reached this point. */
 int nnet_burn(nnet_handle h, const nnet_burn_args* args, void* stream);
 /* One persistent launch over up to three sub-batches of different networks (same EOS and
- * solver): threads drain the net86, net87 and net14 work queues in that order, so the
- * costliest particles start first.  Same semantics per particle as nnet_burn. */
+ * solver): warps (batched layout; threads for the dense solver or the thread layout) drain
+ * the net86, net87 and net14 work queues in that order, so the costliest particles start
+ * first.  Same semantics and, per layout, the same results per particle as nnet_burn. */
 int nnet_burn_batch(nnet_handle h, const nnet_burn_args* batches, int count, void* stream);
 /* Copy the statistics of the last nnet_burn issued on this handle (synchronises the
  * handle's internal stream). */

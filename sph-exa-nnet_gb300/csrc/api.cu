@@ -546,7 +546,9 @@ extern "C" int nnet_burn_batch(nnet_handle h, const nnet_burn_args* batches, int
     if (total == 0) return NNET_SUCCESS;
     NNET_CUDA(cudaSetDevice(h->device));
     cudaStream_t st = (cudaStream_t)stream;
-    KernelInfo   ki = multiKernel(batches[0].eos, batches[0].solver);
+    const bool   tpp = batches[0].solver == NNET_SOLVER_DENSE_FP64 || h->layout == NNET_LAYOUT_THREAD;
+    KernelInfo   ki  = tpp ? multiKernel(batches[0].eos, batches[0].solver)
+                           : batchMultiKernel(batches[0].eos, batches[0].solver == NNET_SOLVER_MIXED);
     for (int ni = 0; ni < 3; ++ni)
         if (mp.active[ni] && ki.maxNnz && h->nets[ni].plan.nnz > ki.maxNnz)
             return fail(NNET_ERR_TOO_LARGE, "sparse factor does not fit the kernel's storage");
@@ -563,7 +565,7 @@ extern "C" int nnet_burn_batch(nnet_handle h, const nnet_burn_args* batches, int
     double*  sc     = h->ws.scratch;
     size_t   stride = slots;
     void*    args[] = {&mp, &hv, &sc, &stride};
-    NNET_CUDA(cudaLaunchKernel(ki.func, dim3((unsigned)blocks), dim3(ki.block), args, 0, st));
+    NNET_CUDA(cudaLaunchKernel(ki.func, dim3((unsigned)blocks), dim3(ki.block), args, ki.smem, st));
     h->lastStream = st;
     h->lastMulti  = true;
     return NNET_SUCCESS;

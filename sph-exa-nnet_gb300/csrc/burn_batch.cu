@@ -16,6 +16,7 @@
 //   S3 (lanes)     acceptance, rejection and timestep control; release / replace
 // Abundances live in per-slot global scratch (contiguous per slot, L2-resident); the slot
 // table and one Newton system per warp live in shared memory.
+#include "burn_multi.hpp"
 #include "launch.hpp"
 #include "warp_system.cuh"
 
@@ -299,17 +300,22 @@ __device__ void slotRates(const NetView& nv, WarpSmem<NET, MIXED>& S, const doub
 
 } // namespace
 
+template<int NET, bool MIXED>
+constexpr int perWarpDoubles()
+{
+    return WarpSmem<NET, MIXED>::doubles + kSlotFields * 32;
+}
+
+// The whole burn of one network's particles by the calling warp.  wb: this warp's shared
+// memory (perWarpDoubles<NET, MIXED>() or more); VS: scratch doubles per slot (at least
+// 2 * padN<NET>()), slot l of global warp gw at scratch + (gw * 32 + l) * VS, holding Y then Yn.
 template<int NET, int EOS, bool MIXED>
-__global__ void __launch_bounds__(64, 1) burnBatchKernel(BurnParams bp, NetView nv, HelmView hv, double* scratch,
-                                                      size_t /*unused*/)
+__device__ void batchLoop(const BurnParams& bp, const NetView& nv, const HelmView& hv, double* scratch, int VS,
+                          double* wb)
 {
     using D                 = WDims<NET>;
     constexpr int NP        = padN<NET>();
-    constexpr int VS        = 2 * NP; // per-slot abundances: Y (substep start), then Yn (iterate)
-    constexpr int perWarp   = WarpSmem<NET, MIXED>::doubles + kSlotFields * 32;
-    extern __shared__ __align__(16) double smem[];
     const int             lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    double*               wb   = smem + (size_t)warp * perWarp;
     WarpSmem<NET, MIXED>  S(wb);
     double*               sc   = wb + WarpSmem<NET, MIXED>::doubles;
     const size_t          gw   = (size_t)blockIdx.x * (blockDim.x >> 5) + warp;
@@ -521,15 +527,48 @@ __global__ void __launch_bounds__(64, 1) burnBatchKernel(BurnParams bp, NetView 
     }
 }
 
+template<int NET, int EOS, bool MIXED>
+__global__ void __launch_bounds__(64, 1) burnBatchKernel(BurnParams bp, NetView nv, HelmView hv, double* scratch,
+                                                      size_t /*unused*/)
+{
+    extern __shared__ __align__(16) double smem[];
+    double* wb = smem + (size_t)(threadIdx.x >> 5) * perWarpDoubles<NET, MIXED>();
+    batchLoop<NET, EOS, MIXED>(bp, nv, hv, scratch, 2 * padN<NET>(), wb);
+}
+
+// One launch over sub-batches of different networks (the uneven mixed workload): every warp
+// drains the net86 queue, then net87, then net14, so the expensive particles start first and
+// the cheap ones fill the tail.  A warp changes network once all its lanes are idle.
+template<int EOS, bool MIXED>
+__global__ void __launch_bounds__(64, 1) burnBatchMultiKernel(MultiParams mp, HelmView hv, double* scratch,
+                                                           size_t /*unused*/)
+{
+    extern __shared__ __align__(16) double smem[];
+    double*       wb = smem + (size_t)(threadIdx.x >> 5) * perWarpDoubles<87, MIXED>();
+    constexpr int VS = 2 * padN<87>();
+    if (mp.active[1]) batchLoop<86, EOS, MIXED>(mp.bp[1], mp.nv[1], hv, scratch, VS, wb);
+    if (mp.active[2]) batchLoop<87, EOS, MIXED>(mp.bp[2], mp.nv[2], hv, scratch, VS, wb);
+    if (mp.active[0]) batchLoop<14, EOS, MIXED>(mp.bp[0], mp.nv[0], hv, scratch, VS, wb);
+}
+
 namespace
 {
 template<int NET, int EOS, bool MIXED>
 KernelInfo batchInfo()
 {
-    constexpr size_t perWarp = WarpSmem<NET, MIXED>::doubles + kSlotFields * 32;
     // lanesPerParticle = 32: a small batch is spread one particle per warp over the grid
     return {(const void*)burnBatchKernel<NET, EOS, MIXED>, (size_t)2 * padN<NET>(), 64, WDims<NET>::NNZ,
-            2 * perWarp * sizeof(double), 32};
+            2 * perWarpDoubles<NET, MIXED>() * sizeof(double), 32};
+}
+
+template<int EOS, bool MIXED>
+KernelInfo batchMultiInfo()
+{
+    static_assert(perWarpDoubles<87, MIXED>() >= perWarpDoubles<86, MIXED>() &&
+                      perWarpDoubles<87, MIXED>() >= perWarpDoubles<14, MIXED>(),
+                  "net87 has the largest warp layout");
+    return {(const void*)burnBatchMultiKernel<EOS, MIXED>, (size_t)2 * padN<87>(), 64, WDims<87>::NNZ,
+            2 * perWarpDoubles<87, MIXED>() * sizeof(double), 32};
 }
 
 template<bool MIXED>
@@ -544,6 +583,12 @@ KernelInfo pickBatch(int net, int eos)
 KernelInfo batchKernel(int net, int eos, int mixed)
 {
     return mixed ? pickBatch<true>(net, eos) : pickBatch<false>(net, eos);
+}
+
+KernelInfo batchMultiKernel(int eos, int mixed)
+{
+    if (mixed) return eos ? batchMultiInfo<1, true>() : batchMultiInfo<0, true>();
+    return eos ? batchMultiInfo<1, false>() : batchMultiInfo<0, false>();
 }
 
 } // namespace nnet_gb300

@@ -20,5 +20,6 @@ KernelInfo denseKernel(int net, int eos);
 KernelInfo sparseKernel(int net, int eos, int mixed);
 KernelInfo warpKernel(int net, int eos, int mixed);  // one warp per particle
 KernelInfo batchKernel(int net, int eos, int mixed); // 32 particles per warp in lockstep
+KernelInfo batchMultiKernel(int eos, int mixed);     // the same over net86, net87, net14 sub-batches
 
 } // namespace nnet_gb300

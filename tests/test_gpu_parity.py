@@ -231,7 +231,7 @@ def test_helmholtz_eos_batch(ctx, port):
         assert rel.max() < 1e-9, (name, rel.max())
 
 
-@pytest.mark.parametrize("solver", ["mixed", "dense"])
+@pytest.mark.parametrize("solver", ["mixed", "sparse", "dense"])
 def test_mixed_network_single_launch(ctx, solver):
     """c3-shaped mix in one launch equals separate per-network burns bit for bit."""
     import torch
@@ -247,14 +247,9 @@ def test_mixed_network_single_launch(ctx, solver):
     st = ctx.stats()
     assert sum(st["status"].values()) == 6000
     for w, b in zip(parts, one):
-        g = gpu_burn(ctx, w, solver)
-        if solver == "mixed":
-            # another kernel instantiation: the FP32 solve may round differently, so the
-            # single-launch results are held to the parity tolerance instead of bit equality
-            check(w, g, (b["Y"].cpu().numpy(), b["T"].cpu().numpy(), g[2], b["status"].cpu().numpy()))
-        else:
-            assert np.array_equal(b["Y"].cpu().numpy(), g[0]) and np.array_equal(b["T"].cpu().numpy(), g[1])
-            assert np.array_equal(b["status"].cpu().numpy(), g[3])
+        g = gpu_burn(ctx, w, solver)  # same per-particle code as the single launch: bit-identical
+        assert np.array_equal(b["Y"].cpu().numpy(), g[0]) and np.array_equal(b["T"].cpu().numpy(), g[1])
+        assert np.array_equal(b["status"].cpu().numpy(), g[3])
 
 
 def test_text_table_loader_matches_binary(ctx, tmp_path):

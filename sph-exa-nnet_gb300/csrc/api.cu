@@ -87,6 +87,19 @@ int uploadNetwork(int net, NetBuffer& b)
     const size_t oBE = putd(BE, N), oZ = putd(Z, net == 14 ? 14 : 87), oZ53 = putd(z53.data(), N);
     const size_t oZf = putd(zf.data(), zf.size());
     const size_t oFit = putd(fit, nfit), oQ = putd(q, nq), oCh = putd(choose, nchoose);
+    // partition-function ratio of every fitted rate per temperature range (the same IEEE
+    // quotient the rate evaluation forms, computed once): net14 [10][24], net86 [150][24]
+    std::vector<double> part;
+    if (net == 14)
+        for (int i = 4; i < 14; ++i)
+            for (int kb = 0; kb < 24; ++kb)
+                part.push_back(choose[(i - 4) * 24 + kb] / choose[(i + 1 - 4) * 24 + kb]);
+    else
+        for (int i = 7; i < 157; ++i)
+            for (int kb = 0; kb < 24; ++kb)
+                part.push_back(choose[(net86_main_reactant[i] - 5) * 24 + kb] /
+                               choose[(net86_main_product[i] - 5) * 24 + kb]);
+    const size_t oPart = putd(part.data(), part.size());
     const size_t oLT = putd(net87_electron_log_temp, NET87_ELECTRON_NTEMP);
     const size_t oLR = putd(net87_electron_log_rho, NET87_ELECTRON_NRHO);
     const size_t oER = putd(net87_electron_rate, (size_t)NET87_ELECTRON_NTEMP * NET87_ELECTRON_NRHO * NET87_ELECTRON_NC);
@@ -135,7 +148,7 @@ int uploadNetwork(int net, NetBuffer& b)
     v.net = net, v.nspec = N, v.nreact = R;
     v.rbeg = I + oRb, v.rspec = I + oRs, v.rcnt = I + oRc, v.pbeg = I + oPb, v.pspec = I + oPs, v.pcnt = I + oPc;
     v.BE = D + oBE, v.Z = D + oZ, v.z53 = D + oZ53, v.fit = D + oFit, v.q = D + oQ, v.choose = D + oCh;
-    v.zFac = D + oZf;
+    v.zFac = D + oZf, v.part = D + oPart;
     v.mainReactant = I + oMr, v.secondaryReactant = I + oSr, v.mainProduct = I + oMp;
     v.eLogT = D + oLT, v.eLogRho = D + oLR, v.eRate = D + oER;
     SparseView& w = v.sp;

@@ -216,8 +216,10 @@ __device__ void slotRates(const NetView& nv, WarpSmem<NET, MIXED>& S, const doub
     constexpr int NS = NET == 14 ? 14 : 86;
     for (int i = lane; i < NS; i += 32)
     {
-        S.BE[i] = cf.be(nv, i);
-        S.mu[i] = (NET != 14 && i == 1) ? 0. : cf.mu(nv, i);
+        double be, mu;
+        cf.beMu(nv, i, be, mu);
+        S.BE[i] = be;
+        S.mu[i] = (NET != 14 && i == 1) ? 0. : mu; // neutrons carry no screening
     }
     __syncwarp();
     FitT v;
@@ -239,8 +241,7 @@ __device__ void slotRates(const NetView& nv, WarpSmem<NET, MIXED>& S, const doub
             const double q   = __ldg(nv.q + i - 4);
             const double dmu = S.mu[i - 1] + S.mu[0] - S.mu[i];
             const double e = exp(f0 + coef + dmu), de = e * (dcoef - dmu * twoT);
-            const double l = __ldg(nv.choose + (i - 4) * 24 + kb) / __ldg(nv.choose + (i + 1 - 4) * 24 + kb) *
-                             exp(coef + f7 - q * val1 + val2);
+            const double l = __ldg(nv.part + (i - 4) * 24 + kb) * exp(coef + f7 - q * val1 + val2);
             S.f[i - 1] = e, S.df[i - 1] = de;
             S.f[16 + i - 1] = l, S.df[16 + i - 1] = l * (dcoef + q * val3 + val4);
         }
@@ -258,7 +259,7 @@ __device__ void slotRates(const NetView& nv, WarpSmem<NET, MIXED>& S, const doub
                                  1e-9;
             const int    mr = __ldg(nv.mainReactant + i), sr = __ldg(nv.secondaryReactant + i),
                       mp = __ldg(nv.mainProduct + i);
-            const double part = __ldg(nv.choose + (mr - 5) * 24 + kb) / __ldg(nv.choose + (mp - 5) * 24 + kb);
+            const double part = __ldg(nv.part + (i - 7) * 24 + kb);
             const double q    = __ldg(nv.q + i - 7);
             const double dmu  = S.mu[mr] + S.mu[sr] - S.mu[mp];
             const double sdmu = i >= 137 ? dmu : 0.;

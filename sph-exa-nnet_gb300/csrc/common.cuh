@@ -76,6 +76,7 @@ struct NetView
     // per species i: sqrt(z53), sqrt(sqrt(z53)), z53^1.9885, log(z53) (fast rate forms)
     const double* zFac;
     const double *fit, *q, *choose;
+    const double* part; // choose-ratio of fitted rate r in temperature range kb at [r * 24 + kb]
     const int *   mainReactant, *secondaryReactant, *mainProduct;
     const double *eLogT, *eLogRho, *eRate;
     SparseView    sp;

@@ -59,6 +59,26 @@ struct CoulombFast
         const double s2 = gq * __ldg(f + 1);
         return -.898004 * g + 4. * (.96786 * s2 - .220703 / s2) + -.86097 * (gl + __ldg(f + 3)) - 2.520058332;
     }
+    // be(nv, i) and mu(nv, i) together: the same values, with the shared loads and quotient once
+    __device__ __forceinline__ void beMu(const NetView& nv, int i, double& beOut, double& muOut) const
+    {
+        const double  g = gam * __ldg(nv.z53 + i);
+        const double* f = nv.zFac + 4 * i;
+        double        fn;
+        if (g > 1)
+        {
+            const double s = gq * __ldg(f + 1), q = .220703 / s;
+            fn             = -.898004 * g + .96786 * s + q + -.86097;
+            muOut          = -.898004 * g + 4. * (.96786 * s - q) + -.86097 * (gl + __ldg(f + 3)) - 2.520058332;
+        }
+        else
+        {
+            const double a = gs * __ldg(f), b = gp * __ldg(f + 2);
+            fn             = -.5 * 1.7320508075688772 * g * a + .29561 * b;
+            muOut          = -(1. / 1.7320508075688772) * g * a + b * .29561 / 1.9885;
+        }
+        beOut = __ldg(nv.BE + i) + corr - nakbt * fn;
+    }
 };
 
 __device__ __forceinline__ void screenFast(double& e, double& de, double dmu, double T)

@@ -48,6 +48,8 @@ def parse():
                     help="requests of the served-stream leg (0 disables it)")
     ap.add_argument("--serve-plain-requests", type=int, default=8,
                     help="requests of the plain-FP64 served-stream comparison (0 disables it)")
+    ap.add_argument("--workload", default="c2",
+                    help="c2 (default line), or c1 / c3 / c4 for the other configurations (one GPU)")
     return ap.parse_args()
 
 
@@ -165,6 +167,10 @@ def main():
     import workloads
 
     rank, world, local = dist_info()
+    if args.workload != "c2":
+        if rank == 0:
+            run_workload(args)
+        return
     if world > 1:
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
@@ -319,6 +325,76 @@ def main():
     ctx.close()
     if world > 1:
         dist.destroy_process_group()
+
+
+# ---------------------------------------------------------------- other configurations
+def run_workload(args):
+    """One JSON line for configuration c1, c3 or c4 on one GPU: particle-burns/s of the device-
+    resident burn (state restored from a pristine HBM copy inside each timed step, inputs larger
+    than L2 except c1).  Their errors against the oracle are the parity tests' (tests/).
+      c1  net14 + ideal gas, 4,096 particles (the reference's CPU-runnable case)
+      c3  2,097,152 particles, 50 % net86 / 30 % net87 / 20 % net14, one nnet_burn_batch launch
+      c4  net87 + Helmholtz, 2,097,152 particles, mixed-precision solver beside the FP64 one"""
+    import torch
+    import nnet_gb300 as nn
+    import workloads
+    dev = torch.device("cuda", 0)
+    ctx = nn.Context(0)
+    stream = torch.cuda.current_stream(dev)
+    name = args.workload
+    solver = args.solver or ("mixed" if name == "c4" else "sparse")
+    parts = workloads.make(name) if name != "c3" else workloads.make("c3")
+    parts = parts if isinstance(parts, list) else [parts]
+    dev_parts = []
+    for w in parts:
+        dev_parts.append(dict(w=w, Y0=torch.tensor(w["Y"], device=dev), T0=torch.tensor(w["T"], device=dev),
+                              dt0=torch.tensor(w["dt"], device=dev), rho=torch.tensor(w["rho"], device=dev),
+                              st=torch.empty(w["T"].size, dtype=torch.int32, device=dev)))
+    for d in dev_parts:
+        d["Y"], d["T"], d["dt"] = torch.empty_like(d["Y0"]), torch.empty_like(d["T0"]), torch.empty_like(d["dt0"])
+    P = sum(w["T"].size for w in parts)
+
+    def step(sv):
+        for d in dev_parts:
+            d["Y"].copy_(d["Y0"]), d["T"].copy_(d["T0"]), d["dt"].copy_(d["dt0"])
+        if len(dev_parts) > 1:
+            ctx.burn_batch([dict(network=d["w"]["net"], Y=d["Y"], T=d["T"], rho=d["rho"], dt=d["dt"],
+                                 hydro_dt=d["w"]["hydro_dt"], status=d["st"]) for d in dev_parts],
+                           solver=sv, eos=nn.EOS_HELMHOLTZ, max_iter=args.max_iter, stream=stream)
+        else:
+            d, w = dev_parts[0], parts[0]
+            ctx.burn(w["net"], d["Y"], d["T"], d["rho"], d["dt"], w["hydro_dt"], eos=w["eos"], mu=w["mu"],
+                     solver=sv, status=d["st"], max_iter=args.max_iter, stream=stream)
+
+    def timed(sv):
+        for _ in range(args.warmup):
+            step(sv)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with ClockSampler(0) as clk:
+            e0.record(stream)
+            for _ in range(args.steps):
+                step(sv)
+            e1.record(stream)
+            torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / args.steps, ctx.stats(), clk.summary()
+
+    ms, stats, clocks = timed(solver)
+    line = {"metric": METRIC, "value": P / (ms / 1e3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": f"synthetic (seeded, workload {name} distributions)",
+            "config": {"workload": {"c1": "net14+ideal gas c1", "c3": "net86/net87/net14 mix c3 (one launch)",
+                                    "c4": "net87+helmholtz c4"}[name], "particles": P, "solver": solver,
+                       "newton_iterations_per_step": stats["newton_iterations"], "status_counts": stats["status"],
+                       "refinement_steps": stats["refinement_steps"], "fp64_fallbacks": stats["fp64_fallbacks"]},
+            "gpu_launches": args.steps, "clocks": clocks}
+    if name == "c4" and solver != "sparse":
+        ms2, stats2, _ = timed("sparse")
+        line["fp64_sparse"] = {"value": P / (ms2 / 1e3), "unit": UNIT, "ms_per_step": ms2,
+                               "newton_iterations_per_step": stats2["newton_iterations"],
+                               "fp64_fallbacks_mixed": stats["fp64_fallbacks"]}
+    print(json.dumps(line), flush=True)
+    ctx.close()
 
 
 def serve_requests(n, seed, scale=1):

@@ -252,6 +252,23 @@ def test_mixed_network_single_launch(ctx, solver):
         assert np.array_equal(b["status"].cpu().numpy(), g[3])
 
 
+@pytest.mark.parametrize("solver", ["sparse", "mixed"])
+def test_c3_single_launch_vs_oracle(ctx, port, solver):
+    """The c3 mix (bimodal temperatures, three networks) in one nnet_burn_batch launch
+    against the oracle, per network."""
+    import torch
+    dev = torch.device("cuda:0")
+    parts = workloads.make_mixed(3000, 56)
+    one = [dict(network=w["net"], Y=torch.tensor(w["Y"], device=dev), T=torch.tensor(w["T"], device=dev),
+                rho=torch.tensor(w["rho"], device=dev), dt=torch.tensor(w["dt"], device=dev), hydro_dt=w["hydro_dt"],
+                status=torch.zeros(w["T"].size, dtype=torch.int32, device=dev)) for w in parts]
+    ctx.burn_batch(one, solver=solver, max_iter=20000)
+    torch.cuda.synchronize()
+    for w, b in zip(parts, one):
+        o = port.burn(w["net"], w["Y"], w["T"], w["rho"], w["dt"], w["hydro_dt"], w["eos"], w["mu"], max_iter=20000)
+        check(w, (b["Y"].cpu().numpy(), b["T"].cpu().numpy(), None, b["status"].cpu().numpy()), o)
+
+
 def test_text_table_loader_matches_binary(ctx, tmp_path):
     """The reference-format text table (helmholtz.cpp:100-137) loads to the same EOS."""
     import torch

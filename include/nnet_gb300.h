@@ -223,12 +223,18 @@ int nnet_measure_fp64_peak(int device, double* tflops);
  * device memory all belongs to their own arena allocator, or that cannot afford the device-wide
  * synchronisation a cudaMalloc may cause).  No counterpart in the reference.  Same arguments
  * and results as nnet_burn with the batched layout; sparse and mixed solvers only.  Allocates
- * nothing: its slot scratch (5.5 MiB, 4096 particle slots) and counters are fixed arrays that
+ * nothing: its slot scratch (7.2 MiB, 4096 particle slots) and counters are fixed arrays that
  * every GPU loading the library holds until exit; the grid is capped to them, so any number of
  * particles is accepted.  The first call on a device looks the arrays up (make it before any
  * stream capture).  Calls share the arrays: calls that overlap on the GPU race, and
  * nnet_get_stats does not report these calls. */
 int nnet_burn_noalloc(nnet_handle h, const nnet_burn_args* args, void* stream);
+
+/* Batched layout: particles in flight per warp, 1..32 (default 32; no reference counterpart,
+ * chosen by the autotuner).  Fewer slots shorten each particle's time per Newton iteration
+ * (the warp serves fewer systems per round) at the price of less sharing of the per-particle
+ * scalar work. */
+int nnet_set_batch_slots(nnet_handle h, int slots);
 
 /* Select the particle layout of the sparse and mixed solvers for later nnet_burn calls on
  * `h` (nnet_layout; no reference counterpart: chosen by the autotuner). */

@@ -512,6 +512,7 @@ int nnet_gb300::launchBurn(nnet_context* h, const nnet_burn_args* a, Workspace& 
     fillParams(a, ws.counters, bp);
     if (rs) bp.rs = *rs;
     bp.sliceIters = sliceIters, bp.segOf = nullptr, bp.segFinished = segFinished;
+    bp.laneSlots  = h->laneSlots;
 
     NNET_CUDA(cudaMemsetAsync(ws.counters, 0, kCounters * sizeof(unsigned long long), st));
     NetView  nv     = h->nets[ni].view;
@@ -520,6 +521,14 @@ int nnet_gb300::launchBurn(nnet_context* h, const nnet_burn_args* a, Workspace& 
     size_t   stride = slots;
     void*    args[] = {&bp, &nv, &hv, &sc, &stride};
     NNET_CUDA(cudaLaunchKernel(ki.func, dim3((unsigned)blocks), dim3(ki.block), args, ki.smem, st));
+    return NNET_SUCCESS;
+}
+
+extern "C" int nnet_set_batch_slots(nnet_handle h, int slots)
+{
+    if (!h) return fail(NNET_ERR_INVALID, "null handle");
+    if (slots < 1 || slots > 32) return fail(NNET_ERR_INVALID, "slots per warp must be in 1..32");
+    h->laneSlots = slots;
     return NNET_SUCCESS;
 }
 
@@ -572,6 +581,7 @@ extern "C" int nnet_burn_batch(nnet_handle h, const nnet_burn_args* batches, int
     {
         const int ni = netIndex(batches[k].network);
         fillParams(batches + k, h->ws.counters + kNetCounters * (ni + 1), mp.bp[ni]);
+        mp.bp[ni].laneSlots = h->laneSlots;
     }
     NNET_CUDA(cudaMemsetAsync(h->ws.counters, 0, kCounters * sizeof(unsigned long long), st));
     HelmView hv     = h->helm;

@@ -14,8 +14,8 @@
 //   S2 (lanes)     EOS and every temperature/density-only rate factor into the slot table
 //   V2 (per slot)  rates, fluxes, system, sparse LU solve, Newton candidate
 //   S3 (lanes)     acceptance, rejection and timestep control; release / replace
-// Abundances live in per-slot global scratch (contiguous per slot, L2-resident); the slot
-// table and one Newton system per warp live in shared memory.
+// Abundances and the slot table live in per-warp global scratch (L2-resident); one Newton
+// system per warp lives in shared memory.
 #include "burn_multi.hpp"
 #include "launch.hpp"
 #include "warp_system.cuh"
@@ -26,7 +26,7 @@ namespace nnet_gb300
 namespace
 {
 
-// per-slot scalars, field-major in shared memory: field f of slot l at sc[f * 32 + l]
+// per-slot scalars, field-major in the warp's global scratch: field f of slot l at sc[f * 32 + l]
 enum SlotField : int
 {
     fT, fTth, fRho, fDrho, fDt, fCv, fDpdT,
@@ -304,12 +304,13 @@ __device__ void slotRates(const NetView& nv, WarpSmem<NET, MIXED>& S, const doub
 template<int NET, bool MIXED>
 constexpr int perWarpDoubles()
 {
-    return WarpSmem<NET, MIXED>::doubles + kSlotFields * 32;
+    return WarpSmem<NET, MIXED>::doubles;
 }
 
 // The whole burn of one network's particles by the calling warp.  wb: this warp's shared
-// memory (perWarpDoubles<NET, MIXED>() or more); VS: scratch doubles per slot (at least
-// 2 * padN<NET>()), slot l of global warp gw at scratch + (gw * 32 + l) * VS, holding Y then Yn.
+// memory (perWarpDoubles<NET, MIXED>() or more); VS: abundance doubles per slot (at least
+// 2 * padN<NET>()).  Global warp gw owns scratch + gw * 32 * (VS + kSlotFields): its 32 slots'
+// abundances (slot l at l * VS: Y then Yn), then its slot table (32 * kSlotFields).
 template<int NET, int EOS, bool MIXED>
 __device__ void batchLoop(const BurnParams& bp, const NetView& nv, const HelmView& hv, double* scratch, int VS,
                           double* wb)
@@ -318,16 +319,18 @@ __device__ void batchLoop(const BurnParams& bp, const NetView& nv, const HelmVie
     constexpr int NP        = padN<NET>();
     const int             lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     WarpSmem<NET, MIXED>  S(wb);
-    double*               sc   = wb + WarpSmem<NET, MIXED>::doubles;
     const size_t          gw   = (size_t)blockIdx.x * (blockDim.x >> 5) + warp;
-    double*               vec0 = scratch + gw * 32 * VS; // slot l at vec0 + l * VS
+    double*               vec0 = scratch + gw * 32 * (size_t)(VS + kSlotFields); // slot l at vec0 + l * VS
+    double*               sc   = vec0 + 32 * VS;
     const SparseView&     sp   = nv.sp;
 
     // spread a small batch over every warp of the grid before filling warps
     const size_t  warps  = (size_t)gridDim.x * (blockDim.x >> 5);
     const size_t  first  = (bp.P + warps - 1) / warps;
+    // particles in flight per warp (fewer shorten each particle's iteration latency)
+    const size_t  spw    = bp.laneSlots > 0 && bp.laneSlots < 32 ? (size_t)bp.laneSlots : 32;
     ParticleState s;
-    bool          has = (size_t)lane < first && acquireLane(bp, s);
+    bool          has = (size_t)lane < (first < spw ? first : spw) && acquireLane(bp, s);
     int           act = has ? ACT_LOAD : 0;
     size_t        pw  = 0;
     double        Tth = 0, rhoT = 0, used = 0, abar = 0, zbar = 0, yElec = 0, xT = 0;
@@ -558,8 +561,8 @@ template<int NET, int EOS, bool MIXED>
 KernelInfo batchInfo()
 {
     // lanesPerParticle = 32: a small batch is spread one particle per warp over the grid
-    return {(const void*)burnBatchKernel<NET, EOS, MIXED>, (size_t)2 * padN<NET>(), 64, WDims<NET>::NNZ,
-            2 * perWarpDoubles<NET, MIXED>() * sizeof(double), 32};
+    return {(const void*)burnBatchKernel<NET, EOS, MIXED>, (size_t)2 * padN<NET>() + kSlotFields, 64,
+            WDims<NET>::NNZ, 2 * perWarpDoubles<NET, MIXED>() * sizeof(double), 32};
 }
 
 template<int EOS, bool MIXED>
@@ -568,8 +571,8 @@ KernelInfo batchMultiInfo()
     static_assert(perWarpDoubles<87, MIXED>() >= perWarpDoubles<86, MIXED>() &&
                       perWarpDoubles<87, MIXED>() >= perWarpDoubles<14, MIXED>(),
                   "net87 has the largest warp layout");
-    return {(const void*)burnBatchMultiKernel<EOS, MIXED>, (size_t)2 * padN<87>(), 64, WDims<87>::NNZ,
-            2 * perWarpDoubles<87, MIXED>() * sizeof(double), 32};
+    return {(const void*)burnBatchMultiKernel<EOS, MIXED>, (size_t)2 * padN<87>() + kSlotFields, 64,
+            WDims<87>::NNZ, 2 * perWarpDoubles<87, MIXED>() * sizeof(double), 32};
 }
 
 template<bool MIXED>

@@ -141,6 +141,7 @@ struct BurnParams
     long long           sliceIters;
     const int*          segOf;
     unsigned long long* segFinished;
+    int                 laneSlots; // batched layout: particles in flight per warp (0 = 32)
 };
 
 } // namespace nnet_gb300

@@ -62,4 +62,5 @@ struct nnet_context
     cudaStream_t           lastStream = nullptr;
     bool                   lastMulti  = false; // last launch was nnet_burn_batch
     int                    layout     = NNET_LAYOUT_AUTO;
+    int                    laneSlots  = 32; // batched layout: particles in flight per warp
 };

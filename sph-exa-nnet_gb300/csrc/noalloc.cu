@@ -10,7 +10,7 @@
 // nothing; the caller passes inputs and outputs exactly as to nnet_burn.
 //
 // Limits and rules:
-//   * the arrays hold kSlots particle slots of the largest network (5.5 MiB of scratch) and are
+//   * the arrays hold kSlots particle slots of the largest network (7.2 MiB of scratch) and are
 //     reserved on every GPU that loads the library, until the process exits;
 //   * scratch does not grow with the number of particles: the persistent grid is capped to the
 //     array's slots and the work queue feeds any number of particles through them; a launch whose
@@ -32,7 +32,7 @@ namespace
 using namespace nnet_gb300;
 
 constexpr size_t kSlots        = 4096; // particle slots in flight at most
-constexpr size_t kSlotDoubles  = 176;  // largest per-slot need of the batched kernels (net86, net87)
+constexpr size_t kSlotDoubles  = 230;  // largest per-slot need of the batched kernels (net86, net87)
 constexpr size_t kScratch      = kSlots * kSlotDoubles;
 constexpr int    kCounterWords = 16; // queue head + statistics (BurnParams::stats)
 
@@ -103,10 +103,11 @@ extern "C" int nnet_burn_noalloc(nnet_handle h, const nnet_burn_args* a, void* s
     const size_t slots    = blocks * ki.block;
     if (blocks == 0 || slots * ki.perSlot > kScratch)
         return setError(NNET_ERR_TOO_LARGE, "nnet_burn_noalloc: one block of this network's slots exceeds the "
-                                            "fixed scratch array (5.5 MiB)");
+                                            "fixed scratch array (7.2 MiB)");
 
     BurnParams bp;
     fillBurnParams(a, d.counters, bp);
+    bp.laneSlots = h->laneSlots;
     cudaStream_t st = (cudaStream_t)stream;
     if (cudaError_t e = cudaMemsetAsync(d.counters, 0, sizeof(g_counters), st)) return cudaFail(e, "cudaMemsetAsync");
     NetView  nv     = h->nets[ni].view;

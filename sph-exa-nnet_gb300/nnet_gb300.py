@@ -81,6 +81,7 @@ def load_library(path=LIB_PATH):
                                      ctypes.POINTER(I)]
     lib.nnet_measure_fp64_peak.argtypes = [I, ctypes.POINTER(D)]
     lib.nnet_set_layout.argtypes = [P, I]
+    lib.nnet_set_batch_slots.argtypes = [P, I]
     _lib = lib
     return lib
 
@@ -118,6 +119,10 @@ class Context:
     def set_layout(self, layout):
         """Particle layout of the sparse / mixed solvers: "auto", "thread", "warp" or "batched"."""
         _check(_lib.nnet_set_layout(self.handle, LAYOUTS[layout] if isinstance(layout, str) else int(layout)))
+
+    def set_batch_slots(self, slots):
+        """Batched layout: particles in flight per warp (1..32)."""
+        _check(_lib.nnet_set_batch_slots(self.handle, int(slots)))
 
     def close(self):
         if self.handle:

@@ -116,7 +116,7 @@ template<bool use_gpu, class Data, typename Float, class Eos>
 void computeNuclearReactions(Data& n, size_t firstIndex, size_t lastIndex, const Float hydro_dt,
                              const Float previous_dt, const ReactionListTag& reactions,
                              const RatesTag& construct_rates_BE, const Eos& eos, bool use_drhodt,
-                             int solver = NNET_SOLVER_MIXED, nnet_handle h = nullptr)
+                             int solver = NNET_SOLVER_SPARSE_FP64, nnet_handle h = nullptr)
 {
     static_assert(use_gpu, "nnet_gb300 has no CPU path");
     if (reactions.network != construct_rates_BE.network)

@@ -177,7 +177,7 @@ class Context:
         s = torch.cuda.current_stream(self.device) if stream is None else stream
         _check(_lib.nnet_burn(self.handle, ctypes.byref(a), ctypes.c_void_p(s.cuda_stream)))
 
-    def burn_batch(self, batches, solver=SOLVER_MIXED, eos=EOS_HELMHOLTZ, mu=0.0, max_iter=100000, stream=None):
+    def burn_batch(self, batches, solver=SOLVER_SPARSE_FP64, eos=EOS_HELMHOLTZ, mu=0.0, max_iter=100000, stream=None):
         """One launch over sub-batches of different networks.  `batches`: list of dicts with
         keys network, Y, T, rho, dt, hydro_dt and optional status / iterations (CUDA tensors)."""
         import torch
@@ -260,7 +260,7 @@ def default_context(device=0):
 
 
 def compute_nuclear_reactions(n, first, last, hydro_dt, previous_dt, reactions, construct_rates_BE, eos,
-                              use_drhodt=False, solver=SOLVER_MIXED, context=None, status=None,
+                              use_drhodt=False, solver=SOLVER_SPARSE_FP64, context=None, status=None,
                               max_iter=100000):
     """Burn particles [first, last) of `n` over hydro_dt, in place (Y, temp, dt), on the
     current CUDA stream.  Same parameters as computeNuclearReactions
@@ -341,7 +341,7 @@ class Server:
     """Continuous-batching burn server over the C ABI (nnet_server_*).  Requests carry
     host numpy arrays (float64; Y species-major [network, P]); results overwrite them."""
 
-    def __init__(self, context, solver=SOLVER_MIXED, hbm_budget_bytes=150e9, slice_iterations=64,
+    def __init__(self, context, solver=SOLVER_SPARSE_FP64, hbm_budget_bytes=150e9, slice_iterations=64,
                  max_concurrent_requests=8):
         lib = load_library()
         P = ctypes.c_void_p

@@ -125,7 +125,7 @@ int uploadNetwork(int net, NetBuffer& b)
                  oRow0 = putv(sp.row0Pos), oCBeg = putv(sp.cBeg), oCPos = putv(sp.cPos), oCRow = putv(sp.cRow),
                  oSb = putv(sp.sbPos), oSbD = putv(sp.sbDiag);
     // warp-per-particle lists
-    const WarpPlan wp = buildWarpPlan(sp, rbeg, rspec, rcnt, pbeg, pspec, pcnt);
+    const WarpPlan wp = buildWarpPlan(sp, rbeg, rspec, rcnt, pbeg, pspec, pcnt, net == 14 ? kWarpNnzCap14 : kWarpNnzCap86);
     const size_t oSgC = putd(wp.sgCoef.data(), wp.sgCoef.size()), oJgC = putd(wp.jgCoef.data(), wp.jgCoef.size());
     const size_t oUpdB = putv(wp.updBeg), oUpdT = putv(wp.updT), oUpdL = putv(wp.updL), oUpdU = putv(wp.updU),
                  oUcB = putv(wp.ucBeg), oUcP = putv(wp.ucPos), oUcR = putv(wp.ucRow), oSgB = putv(wp.sgBeg),
@@ -138,6 +138,8 @@ int uploadNetwork(int net, NetBuffer& b)
                  oTuL = putv(wp.tuL), oTuU = putv(wp.tuU), oFwB = putv(wp.fwBeg), oFwR = putv(wp.fwRow),
                  oFwE = putv(wp.fwEnt), oFlP = putv(wp.flPos), oFlK = putv(wp.flK), oBwB = putv(wp.bwBeg),
                  oBwR = putv(wp.bwRow), oBwE = putv(wp.bwEnt), oBuP = putv(wp.buPos), oBuK = putv(wp.buK);
+    const size_t oScB = putv(wp.scBeg), oScP = putv(wp.scPos), oScK = putv(wp.scPiv), oTgBA = putv(wp.tgBegA),
+                 oTgPA = putv(wp.tgPosA), oTgUA = putv(wp.tgUpdA), oTuLA = putv(wp.tuLA), oTuUA = putv(wp.tuUA);
     const size_t bytesD = d.size() * sizeof(double), bytes = bytesD + ii.size() * sizeof(int);
     NNET_CUDA(cudaMalloc(&b.mem, bytes));
     NNET_CUDA(cudaMemcpy(b.mem, d.data(), bytesD, cudaMemcpyHostToDevice));
@@ -171,6 +173,9 @@ int uploadNetwork(int net, NetBuffer& b)
     x.tgBeg = I + oTgB, x.tgPos = I + oTgP, x.tgUpd = I + oTgU, x.tuL = I + oTuL, x.tuU = I + oTuU;
     x.fwBeg = I + oFwB, x.fwRow = I + oFwR, x.fwEnt = I + oFwE, x.flPos = I + oFlP, x.flK = I + oFlK;
     x.bwBeg = I + oBwB, x.bwRow = I + oBwR, x.bwEnt = I + oBwE, x.buPos = I + oBuP, x.buK = I + oBuK;
+    x.rhsBase = wp.rhsBase;
+    x.scBeg = I + oScB, x.scPos = I + oScP, x.scPiv = I + oScK, x.tgBegA = I + oTgBA, x.tgPosA = I + oTgPA;
+    x.tgUpdA = I + oTgUA, x.tuLA = I + oTuLA, x.tuUA = I + oTuUA;
     return NNET_SUCCESS;
 }
 

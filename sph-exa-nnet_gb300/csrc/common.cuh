@@ -64,6 +64,9 @@ struct WarpView
     int        nLevels;
     const int *lvBeg, *lvPiv, *lsBeg, *lsPos, *lsPiv, *tgBeg, *tgPos, *tgUpd, *tuL, *tuU;
     const int *fwBeg, *fwRow, *fwEnt, *flPos, *flK, *bwBeg, *bwRow, *bwEnt, *buPos, *buK;
+    // fused forms (WarpPlan::scBeg ... tuUA)
+    int        rhsBase;
+    const int *scBeg, *scPos, *scPiv, *tgBegA, *tgPosA, *tgUpdA, *tuLA, *tuUA;
 };
 
 // Read-only device view of one network definition (reaction list in CSR form, binding

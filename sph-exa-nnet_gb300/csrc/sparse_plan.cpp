@@ -151,7 +151,7 @@ namespace nnet_gb300
 
 namespace
 {
-void buildLevels(const SparsePlan& P, WarpPlan& W)
+void buildLevels(const SparsePlan& P, WarpPlan& W, int rhsBase)
 {
     const int        n = P.n;
     std::vector<int> lev(n, 0);
@@ -204,6 +204,33 @@ void buildLevels(const SparsePlan& P, WarpPlan& W)
         W.tgBeg.push_back((int)W.tgPos.size());
         W.fwBeg.push_back((int)W.fwRow.size());
     }
+    // fused scaling and augmented factorisation
+    W.rhsBase = rhsBase;
+    W.scBeg = {0}, W.tgBegA = {0}, W.tgUpdA = {0};
+    for (int l = 0; l < nl; ++l)
+    {
+        std::map<int, std::vector<std::pair<int, int>>> tgt;
+        for (int k : piv[l])
+        {
+            if (P.lBeg[k] == P.lBeg[k + 1]) W.scPos.push_back(-1), W.scPiv.push_back(k);
+            for (int e = P.lBeg[k]; e < P.lBeg[k + 1]; ++e)
+            {
+                W.scPos.push_back(P.lPos[e]), W.scPiv.push_back(k);
+                for (int u = P.uBeg[k]; u < P.uBeg[k + 1]; ++u)
+                    tgt[P.tPos[P.tBeg[e] + (u - P.uBeg[k])]].push_back({P.lPos[e], P.uPos[u]});
+                tgt[rhsBase + P.lRow[e]].push_back({P.lPos[e], rhsBase + k});
+            }
+        }
+        for (auto& [t, lst] : tgt)
+        {
+            W.tgPosA.push_back(t);
+            for (auto& pr : lst)
+                W.tuLA.push_back(pr.first), W.tuUA.push_back(pr.second);
+            W.tgUpdA.push_back((int)W.tuLA.size());
+        }
+        W.scBeg.push_back((int)W.scPos.size());
+        W.tgBegA.push_back((int)W.tgPosA.size());
+    }
     // backward: levels last to first; rows above the level's pivots, by U column
     W.bwBeg = {0}, W.bwEnt = {0};
     for (int l = nl - 1; l >= 0; --l)
@@ -225,7 +252,7 @@ void buildLevels(const SparsePlan& P, WarpPlan& W)
 } // namespace
 
 WarpPlan buildWarpPlan(const SparsePlan& P, const int* rbeg, const int* rspec, const int* rcnt, const int* pbeg,
-                       const int* pspec, const int* pcnt)
+                       const int* pspec, const int* pcnt, int rhsBase)
 {
     WarpPlan  W;
     const int n = P.n, N = P.N, R = P.R;
@@ -318,7 +345,7 @@ WarpPlan buildWarpPlan(const SparsePlan& P, const int* rbeg, const int* rspec, c
         if (W.rjBeg[i + 1] - W.rjBeg[i] > WarpPlan::kHeavy) W.rjHeavy.push_back(i);
     for (int i = 0; i < n; ++i)
         if (P.rowBeg[i + 1] - P.rowBeg[i] > WarpPlan::kHeavy) W.rowHeavy.push_back(i);
-    buildLevels(P, W);
+    buildLevels(P, W, rhsBase);
     (void)pspec, (void)pcnt, (void)rcnt;
     return W;
 }

@@ -87,9 +87,22 @@ struct WarpPlan
     int              nLevels = 0;
     std::vector<int> lvBeg, lvPiv, lsBeg, lsPos, lsPiv, tgBeg, tgPos, tgUpd, tuL, tuU;
     std::vector<int> fwBeg, fwRow, fwEnt, flPos, flK, bwBeg, bwRow, bwEnt, buPos, buK;
+    // Fused forms of the same schedule:
+    //   scaling with the reciprocal folded in: scPos / scPiv over scBeg[l] .. scBeg[l+1]
+    //   (every L entry of the level's pivots, plus (-1, k) for a pivot without L entries);
+    //   factorisation with the forward substitution folded in: the right-hand side is
+    //   column `rhsBase` + row of the stored matrix (the kernels keep b right after the
+    //   factor's rhsBase entries), and tgBegA / tgPosA / tgUpdA / tuLA / tuUA list the
+    //   level's targets including the right-hand-side rows.
+    int              rhsBase = 0;
+    std::vector<int> scBeg, scPos, scPiv, tgBegA, tgPosA, tgUpdA, tuLA, tuUA;
 };
 
+// capacity of the factor storage of the warp-cooperative kernels (the right-hand side
+// follows it in shared memory)
+constexpr int kWarpNnzCap14 = 104, kWarpNnzCap86 = 1056;
+
 WarpPlan buildWarpPlan(const SparsePlan& P, const int* rbeg, const int* rspec, const int* rcnt, const int* pbeg,
-                       const int* pspec, const int* pcnt);
+                       const int* pspec, const int* pcnt, int rhsBase);
 
 } // namespace nnet_gb300

@@ -24,7 +24,7 @@ struct WDims
     static constexpr int N   = NET, n = NET + 1;
     static constexpr int R   = NetDims<NET>::R;
     static constexpr int NE  = NET == 14 ? 42 : NET == 86 ? 482 : 486; // reactant entries
-    static constexpr int NNZ = NET == 14 ? 104 : 1056;                 // factor capacity (checked on host)
+    static constexpr int NNZ = NET == 14 ? kWarpNnzCap14 : kWarpNnzCap86; // factor capacity (checked on host)
 };
 
 // shared-memory layout of one warp (doubles; the float factor of the mixed form overlaps
@@ -36,12 +36,12 @@ struct WarpSmem
     static constexpr int oY = 0, oYn = oY + D::N, oF = oYn + D::N, oDF = oF + D::R, oBE = oDF + D::R,
                          oA = oBE + D::N, oB = oA + D::NNZ, oDYdt = oB + D::n, oDYdT = oDYdt + D::N,
                          oJdy = oDYdT + D::N, oTr = oJdy + D::N;
-    static constexpr int floatsD = (D::NNZ + 2 * D::n + 1) / 2;
+    static constexpr int floatsD = (D::NNZ + 3 * D::n + 1) / 2;
     static constexpr int doubles = oTr + (MIXED && floatsD > D::NE ? floatsD : D::NE);
 
     static_assert(4 * D::n <= 2 * D::R + D::N, "solve vectors must fit the flux storage");
     double *Y, *Yn, *f, *df, *BE, *A, *b, *dYdt, *mu, *dYdT, *jdy, *tr, *x, *r, *ipiv, *scale;
-    float * LU, *d, *ipiv32;
+    float * LU, *d, *ipiv32, *x32;
 
     __device__ explicit WarpSmem(double* s)
     {
@@ -50,7 +50,7 @@ struct WarpSmem
         mu = dYdt; // screening potentials live until the rates are done
         // the solve vectors reuse the flux / binding-energy storage, dead after assembly
         x = f, r = f + D::n, ipiv = f + 2 * D::n, scale = f + 3 * D::n;
-        LU = reinterpret_cast<float*>(tr), d = LU + D::NNZ, ipiv32 = d + D::n;
+        LU = reinterpret_cast<float*>(tr), d = LU + D::NNZ, ipiv32 = d + D::n, x32 = ipiv32 + D::n;
     }
 };
 
@@ -201,78 +201,99 @@ __device__ void warpAssemble(const NetView& nv, WarpSmem<NET, MIXED>& S, double 
 __device__ __forceinline__ double recip(double a) { return __drcp_rn(a); }
 __device__ __forceinline__ float  recip(float a) { return __frcp_rn(a); }
 
-template<typename F>
+// Level-scheduled right-looking LU without pivoting, in place (FP64 or FP32).  Per level:
+// the multipliers (each lane forms its pivot's reciprocal itself, so no separate round is
+// needed), then every target's updates in pivot order.  AUG: the right-hand side, stored
+// right after the factor's rhsBase entries, is a column of the matrix, so the forward
+// substitution happens in the same rounds.
+template<typename F, bool AUG>
 __device__ void levelFactor(const SparseView& sp, const WarpView& wv, F* A, F* ipiv, int lane)
 {
+    const int* tgBeg = AUG ? wv.tgBegA : wv.tgBeg;
+    const int* tgPos = AUG ? wv.tgPosA : wv.tgPos;
+    const int* tgUpd = AUG ? wv.tgUpdA : wv.tgUpd;
+    const int* tuL   = AUG ? wv.tuLA : wv.tuL;
+    const int* tuU   = AUG ? wv.tuUA : wv.tuU;
     for (int l = 0; l < wv.nLevels; ++l)
     {
-        for (int q = __ldg(wv.lvBeg + l) + lane; q < __ldg(wv.lvBeg + l + 1); q += 32)
+        for (int e = __ldg(wv.scBeg + l) + lane; e < __ldg(wv.scBeg + l + 1); e += 32)
         {
-            const int k = __ldg(wv.lvPiv + q);
-            ipiv[k]     = recip(A[__ldg(sp.kPiv + k)]);
+            const int k = __ldg(wv.scPiv + e), pos = __ldg(wv.scPos + e);
+            const F   ip = recip(A[__ldg(sp.kPiv + k)]);
+            if (pos >= 0) A[pos] *= ip;
+            ipiv[k] = ip; // lanes of one pivot write the same value
         }
         __syncwarp();
-        for (int e = __ldg(wv.lsBeg + l) + lane; e < __ldg(wv.lsBeg + l + 1); e += 32)
-            A[__ldg(wv.lsPos + e)] *= ipiv[__ldg(wv.lsPiv + e)];
-        __syncwarp();
-        for (int t = __ldg(wv.tgBeg + l) + lane; t < __ldg(wv.tgBeg + l + 1); t += 32)
+        for (int t = __ldg(tgBeg + l) + lane; t < __ldg(tgBeg + l + 1); t += 32)
         {
-            const int pos = __ldg(wv.tgPos + t);
+            const int pos = __ldg(tgPos + t);
             F         a   = A[pos];
-            for (int u = __ldg(wv.tgUpd + t), ue = __ldg(wv.tgUpd + t + 1); u < ue; ++u)
-                a = a - A[__ldg(wv.tuL + u)] * A[__ldg(wv.tuU + u)];
+            for (int u = __ldg(tgUpd + t), ue = __ldg(tgUpd + t + 1); u < ue; ++u)
+                a = a - A[__ldg(tuL + u)] * A[__ldg(tuU + u)];
             A[pos] = a;
         }
         __syncwarp();
     }
 }
 
-// x <- U^-1 L^-1 x with the factor of levelFactor (same level schedule)
+// y <- L^-1 y with the factor of levelFactor (unit lower triangle)
 template<typename F>
-__device__ void levelSolve(const WarpView& wv, const F* A, const F* ipiv, F* x, int lane)
+__device__ void levelForward(const WarpView& wv, const F* A, F* y, int lane)
 {
     for (int l = 0; l < wv.nLevels; ++l)
     {
         for (int r = __ldg(wv.fwBeg + l) + lane; r < __ldg(wv.fwBeg + l + 1); r += 32)
         {
             const int row = __ldg(wv.fwRow + r);
-            F         a   = x[row];
+            F         a   = y[row];
             for (int e = __ldg(wv.fwEnt + r), ee = __ldg(wv.fwEnt + r + 1); e < ee; ++e)
-                a = a - A[__ldg(wv.flPos + e)] * x[__ldg(wv.flK + e)];
-            x[row] = a;
-        }
-        __syncwarp();
-    }
-    for (int li = 0; li < wv.nLevels; ++li)
-    {
-        const int l = wv.nLevels - 1 - li;
-        for (int q = __ldg(wv.lvBeg + l) + lane; q < __ldg(wv.lvBeg + l + 1); q += 32)
-        {
-            const int k = __ldg(wv.lvPiv + q);
-            x[k]        = x[k] * ipiv[k];
-        }
-        __syncwarp();
-        for (int r = __ldg(wv.bwBeg + li) + lane; r < __ldg(wv.bwBeg + li + 1); r += 32)
-        {
-            const int row = __ldg(wv.bwRow + r);
-            F         a   = x[row];
-            for (int e = __ldg(wv.bwEnt + r), ee = __ldg(wv.bwEnt + r + 1); e < ee; ++e)
-                a = a - A[__ldg(wv.buPos + e)] * x[__ldg(wv.buK + e)];
-            x[row] = a;
+                a = a - A[__ldg(wv.flPos + e)] * y[__ldg(wv.flK + e)];
+            y[row] = a;
         }
         __syncwarp();
     }
 }
 
-// FP64: factor A in place, x = A^-1 b
+// x <- U^-1 y (y is consumed): one round per level, last level first; each lane either
+// finishes one of the level's pivots (x_k = y_k / u_kk) or updates one row above them
+// with the same products.
+template<typename F>
+__device__ void levelBackward(const WarpView& wv, const F* A, const F* ipiv, F* y, F* x, int lane)
+{
+    for (int li = 0; li < wv.nLevels; ++li)
+    {
+        const int l = wv.nLevels - 1 - li;
+        const int p0 = __ldg(wv.lvBeg + l), nP = __ldg(wv.lvBeg + l + 1) - p0;
+        const int r0 = __ldg(wv.bwBeg + li), nR = __ldg(wv.bwBeg + li + 1) - r0;
+        for (int t = lane; t < nP + nR; t += 32)
+        {
+            if (t < nP)
+            {
+                const int k = __ldg(wv.lvPiv + p0 + t);
+                x[k]        = y[k] * ipiv[k];
+            }
+            else
+            {
+                const int r = r0 + t - nP, row = __ldg(wv.bwRow + r);
+                F         a = y[row];
+                for (int e = __ldg(wv.bwEnt + r), ee = __ldg(wv.bwEnt + r + 1); e < ee; ++e)
+                {
+                    const int k = __ldg(wv.buK + e);
+                    a           = a - A[__ldg(wv.buPos + e)] * (y[k] * ipiv[k]);
+                }
+                y[row] = a;
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// FP64: factor A in place with b as an extra column, then x = U^-1 (L^-1 b); b is consumed
 template<int NET, bool MIXED>
 __device__ void warpSolve64(const NetView& nv, WarpSmem<NET, MIXED>& S, int lane)
 {
-    levelFactor<double>(nv.sp, nv.wv, S.A, S.ipiv, lane);
-    for (int i = lane; i < WDims<NET>::n; i += 32)
-        S.x[i] = S.b[i];
-    __syncwarp();
-    levelSolve<double>(nv.wv, S.A, S.ipiv, S.x, lane);
+    levelFactor<double, true>(nv.sp, nv.wv, S.A, S.ipiv, lane);
+    levelBackward<double>(nv.wv, S.A, S.ipiv, S.b, S.x, lane);
 }
 
 // rows scaled by powers of two, FP32 factorisation, FP64 residual refinement; returns
@@ -295,7 +316,7 @@ __device__ int warpSolveMixed(const NetView& nv, WarpSmem<NET, true>& S, double 
     for (int p = lane; p < sp.nnz; p += 32)
         S.LU[p] = (float)(S.A[p] * scale[__ldg(sp.posRow + p)]);
     __syncwarp();
-    levelFactor<float>(sp, wv, S.LU, S.ipiv32, lane);
+    levelFactor<float, false>(sp, wv, S.LU, S.ipiv32, lane);
     for (int i = lane; i < D::n; i += 32)
         S.x[i] = 0., S.r[i] = S.b[i];
     __syncwarp();
@@ -304,11 +325,12 @@ __device__ int warpSolveMixed(const NetView& nv, WarpSmem<NET, true>& S, double 
         for (int i = lane; i < D::n; i += 32)
             S.d[i] = (float)(S.r[i] * scale[i]);
         __syncwarp();
-        levelSolve<float>(wv, S.LU, S.ipiv32, S.d, lane);
+        levelForward<float>(wv, S.LU, S.d, lane);
+        levelBackward<float>(wv, S.LU, S.ipiv32, S.d, S.x32, lane);
         bool conv = true;
         for (int i = lane; i < D::n; i += 32)
         {
-            const double di = (double)S.d[i], xi = S.x[i] + di;
+            const double di = (double)S.x32[i], xi = S.x[i] + di;
             const int    o  = __ldg(sp.perm + i);
             const double sc = o == 0 ? T : fabs(S.Y[o - 1]);
             conv &= fabs(di) <= kRefineTol * (fabs(xi) + sc) && isfinite(xi); // an FP32 overflow is not convergence

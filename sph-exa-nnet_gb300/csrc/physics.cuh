@@ -198,7 +198,7 @@ static __device__ EosResult helmholtzEos(const HelmView& hv, double abar_, doubl
     double       z      = pi * 4. / 3.;
     double       s      = z * xni;
     const double dsdd   = z * dxnidd;
-    const double lami   = cbrt((double)1. / s), inv_lami = 1. / lami;
+    const double lami   = pow((double)1. / s, (double)1. / 3.), inv_lami = 1. / lami;
     z                   = -lami / 3;
     const double lamidd = z * dsdd / s;
     const double plasg  = zbar * zbar * esqu * ktinv * inv_lami;
@@ -209,7 +209,7 @@ static __device__ EosResult helmholtzEos(const HelmView& hv, double abar_, doubl
     double ecoul = 0, pcoul = 0, decouldd = 0, decouldt = 0, dpcouldd = 0, dpcouldt = 0;
     if (plasg >= 1.)
     {
-        x           = sqrt(sqrt(plasg));
+        x           = pow(plasg, (double)0.25);
         double y    = avo * ytot1 * kerg;
         ecoul       = y * temp * (a1 * plasg + b1 * x + c1 / x + d1);
         pcoul       = rho * ecoul / 3.;
@@ -326,7 +326,7 @@ struct FitT
     FitT() = default; // fields filled by the caller (values computed elsewhere)
     __device__ explicit FitT(double T)
     {
-        t9 = T / 1.e9, t913 = cbrt(t9), t923 = t913 * t913, t953 = t9 * t923;
+        t9 = T / 1.e9, t913 = pow(t9, 1. / 3.), t923 = t913 * t913, t953 = pow(t9, 5. / 3.);
         t9i = 1.e0 / t9, t9i2 = t9i * t9i, t9i13 = 1.e0 / t913, t9i23 = t9i13 * t9i13, t9i43 = t9i23 * t9i23;
         lt9 = log(t9);
     }
@@ -342,8 +342,6 @@ __device__ __forceinline__ void fitRate(const double* f, const FitT& v, double& 
     deff  = eff * dcoef;
 }
 
-__device__ __forceinline__ double sq(double x) { return x * x; }
-
 // The seven CF88-type special rates shared by net14 and net86 (net14.cpp:153-561,
 // net86.cpp:135-505): triple-alpha (+ reverse), 12C+12C, 12C+16O, 16O+16O,
 // 12C(a,g) (+ reverse), 16O(a,g) (+ reverse).
@@ -356,7 +354,7 @@ static __device__ __noinline__ void specialRates(double T, Special& s)
     {
         const double t9r = T * 1.0e-09, t9 = fmin((double)10., t9r);
         const double t92 = t9 * t9, t93 = t92 * t9, t95 = t92 * t93, t912 = sqrt(t9);
-        const double t913 = cbrt(t9), t923 = t913 * t913, t932 = t9 * t912, t943 = t9 * t913,
+        const double t913 = pow(t9, 1. / 3.), t923 = t913 * t913, t932 = t9 * t912, t943 = t9 * t913,
                      t953 = t9 * t923;
         const double t9i = 1. / t9, t9i13 = 1. / t913, t9i23 = 1. / t923, t9i32 = 1. / t932, t9rm1 = 1. / t9r,
                      t9r32 = t9 * sqrt(t9r);
@@ -375,20 +373,20 @@ static __device__ __noinline__ void specialRates(double T, Special& s)
         s.l3a = s.e3a * (2.e20 * exp(-84.419412e0 * t9i)) * t93;
 
         {
-            const double t9a = t9 / (1. + 0.0396 * t9), t9a13 = cbrt(t9a), t9a56 = t9a / sqrt(t9a13);
+            const double t9a = t9 / (1. + 0.0396 * t9), t9a13 = pow(t9a, 1. / 3.), t9a56 = pow(t9a, 5. / 6.);
             s.e2c = 4.27e+26 * t9a56 * t9i32 * exp(-84.165 / t9a13 - 2.12e-03 * t93);
         }
         s.eco = 0;
         if (T >= 5e8)
         {
-            const double t9ap = t9 / (1. + 0.055 * t9), t9a2p = t9ap * t9ap, t9a13p = cbrt(t9ap),
-                         t9a23p = t9a13p * t9a13p, t9a56ap = t9ap / sqrt(t9a13p);
+            const double t9ap = t9 / (1. + 0.055 * t9), t9a2p = t9ap * t9ap, t9a13p = pow(t9ap, 1. / 3.),
+                         t9a23p = t9a13p * t9a13p, t9a56ap = pow(t9ap, 5. / 6.);
             s.eco = 1.72e+31 * t9a56ap * t9i32 * exp(-106.594 / t9a13p) /
                     (exp(-0.18 * t9a2p) + 1.06e-03 * exp(2.562 * t9a23p));
         }
         s.e2o  = 7.10e+36 * t9i23 * exp(-135.93 * t9i13 - 0.629 * t923 - 0.445 * t943 + 0.0103 * t92);
-        s.ecag = 1.04e+08 / (t92 * sq(1. + 0.0489 * t9i23)) * exp(-32.120 * t9i13 - t92 / 12.222016) +
-                 1.76e+08 / (t92 * sq(1. + 0.2654 * t9i23)) * exp(-32.120 * t9i13) +
+        s.ecag = 1.04e+08 / (t92 * pow(1. + 0.0489 * t9i23, 2.)) * exp(-32.120 * t9i13 - t92 / 12.222016) +
+                 1.76e+08 / (t92 * pow(1. + 0.2654 * t9i23, 2.)) * exp(-32.120 * t9i13) +
                  1.25e+03 * t9i32 * exp(-27.499 * t9i) + 1.43e-02 * t95 * exp(-15.541 * t9i);
         s.lcag = s.ecag * 5.13e+10 * t9r32 * exp(-83.108047 * t9rm1);
         s.eoag = (9.37e+09 * t9i23 * exp(-39.757 * t9i13 - t92 / 2.515396) + 62.1 * t9i32 * exp(-10.297 * t9i) +
@@ -398,7 +396,7 @@ static __device__ __noinline__ void specialRates(double T, Special& s)
     {
         // temperature derivatives, unclamped t9 (net14.cpp:357-561)
         const double t9 = T * 1.0e-09, t92 = t9 * t9, t93 = t92 * t9, t94 = t93 * t9, t95 = t94 * t9;
-        const double t912 = sqrt(t9), t913 = cbrt(t9), t923 = t913 * t913, t932 = t9 * t912,
+        const double t912 = sqrt(t9), t913 = pow(t9, 1. / 3.), t923 = t913 * t913, t932 = t9 * t912,
                      t943 = t9 * t913, t952 = t9 * t932, t953 = t9 * t923;
         const double t9i = 1. / t9, t9i2 = t9i * t9i, t9i13 = 1. / t913, t9i23 = 1. / t923, t9i32 = 1. / t932,
                      t9i43 = 1. / t943, t9i52 = 1. / t952, t9i53 = 1. / t953;
@@ -431,22 +429,22 @@ static __device__ __noinline__ void specialRates(double T, Special& s)
             s.dl3a          = 2.00e20 * exp(vA) * t93 * (dvA * s.e3a + 3. * t9i * s.e3a + s.de3a) * 1.e-9;
         }
         {
-            const double vA = t9 / (1. + .0396 * t9), c3 = cbrt(vA), c6 = sqrt(c3), vA56 = vA / c6;
-            const double vB = -84.165 * (1. / c3) - 2.12e-3 * t93;
-            const double dvA = vA * vA * t9i2, dvB = 28.055 * dvA * (1. / (vA * c3)) - 6.36e-3 * t92;
-            s.de2c = 4.27e26 * t9i32 * exp(vB) * ((1. / c6) * dvA * 5. / 6. - 1.5 * vA56 * t9i + vA56 * dvB) *
+            const double vA = t9 / (1. + .0396 * t9), vA56 = pow(vA, 5. / 6.);
+            const double vB = -84.165 * pow(vA, -1. / 3.) - 2.12e-3 * t93;
+            const double dvA = vA * vA * t9i2, dvB = 28.055 * dvA * pow(vA, -4. / 3.) - 6.36e-3 * t92;
+            s.de2c = 4.27e26 * t9i32 * exp(vB) * (pow(vA, -1. / 6.) * dvA * 5. / 6. - 1.5 * vA56 * t9i + vA56 * dvB) *
                      1.e-9;
         }
         s.deco = 0;
         if (t9 > .5)
         {
-            const double vA = t9 / (1. + .055 * t9), c3 = cbrt(vA), c6 = sqrt(c3), vA56 = vA / c6;
-            const double vB = -106.594 * (1. / c3), vC = -.18 * vA * vA, vD = 2.562 * (c3 * c3);
+            const double vA = t9 / (1. + .055 * t9), vA56 = pow(vA, 5. / 6.);
+            const double vB = -106.594 * pow(vA, -1. / 3.), vC = -.18 * vA * vA, vD = 2.562 * pow(vA, 2. / 3.);
             const double val = exp(vC) + 1.06e-3 * exp(vD);
-            const double dvA = vA * vA * t9i2, dvB = 106.594 * (1. / (vA * c3)) * dvA / 3.;
-            const double dvC = -.36 * vA * dvA, dvD = 1.708 * dvA * (1. / c3);
+            const double dvA = vA * vA * t9i2, dvB = 106.594 * pow(vA, -4. / 3.) * dvA / 3.;
+            const double dvC = -.36 * vA * dvA, dvD = 1.708 * dvA * pow(vA, -1. / 3.);
             const double dval = dvC * exp(vC) + 1.06e-3 * dvD * exp(vD);
-            s.deco = 1.72e31 * t9i32 * ((1. / c6) * dvA * 5. / 6. - 1.5 * vA56 * t9i + vA56 * (dvB - dval / val)) *
+            s.deco = 1.72e31 * t9i32 * (pow(vA, -1. / 6.) * dvA * 5. / 6. - 1.5 * vA56 * t9i + vA56 * (dvB - dval / val)) *
                      exp(vB) / val * 1.e-9;
         }
         {
@@ -455,10 +453,10 @@ static __device__ __noinline__ void specialRates(double T, Special& s)
             s.de2o           = 7.10e36 * exp(vA) * t9i23 * (-t9i * 2. / 3. + dvA) * 1.e-9;
         }
         {
-            const double vB = sq(1. + .0489 * t9i23), vC = -32.120 * t9i13 - sq(t9 / 3.496);
-            const double vD = sq(1. + .2654 * t9i23), vE = -32.120 * t9i13, vF = -27.499 * t9i, vG = -15.541 * t9i;
+            const double vB = pow(1. + .0489 * t9i23, 2), vC = -32.120 * t9i13 - pow(t9 / 3.496, 2.);
+            const double vD = pow(1. + .2654 * t9i23, 2), vE = -32.120 * t9i13, vF = -27.499 * t9i, vG = -15.541 * t9i;
             const double dvB = -(2. + .0978 * t9i23) * (.0326 * t9i53);
-            const double dvC = 32.120 * t9i43 / 3. - 2. * t9 / (3.496 * 3.496);
+            const double dvC = 32.120 * t9i43 / 3. - 2. * t9 / pow(3.496, 2.);
             const double dvD = -(2. + .5308 * t9i23) * (.5308 * t9i53 / 3.);
             const double dvE = 32.120 * t9i43 / 3., dvF = 27.499 * t9i2, dvG = 15.541 * t9i2;
             s.decag = (1.04e8 * exp(vC) * t9i2 * (-2. * t9i + dvC - dvB / vB) / vB +
@@ -467,9 +465,9 @@ static __device__ __noinline__ void specialRates(double T, Special& s)
                       1.e-9;
         }
         {
-            const double vA = -83.108047 * t9i, vB = -39.757 * t9i13 - sq(t9 / 1.586);
+            const double vA = -83.108047 * t9i, vB = -39.757 * t9i13 - pow(t9 / 1.586, 2.);
             const double vC = -10.297 * t9i, vD = -12.226 * t9i, vE = -20.093 * t9i;
-            const double dvA = 83.108047 * t9i2, dvB = 39.757 * t9i43 / 3. - 2. * t9 / (1.586 * 1.586);
+            const double dvA = 83.108047 * t9i2, dvB = 39.757 * t9i43 / 3. - 2. * t9 / pow(1.586, 2.);
             const double dvC = 10.297 * t9i2, dvD = 12.226 * t9i2, dvE = 20.093 * t9i2;
             s.dlcag = 5.13e10 * exp(vA) * (s.decag * t932 + s.ecag * 1.5 * t912 + s.ecag * t932 * dvA) * 1.e-9;
             s.deoag = (9.37e9 * exp(vB) * (-t9i53 * 2. / 3. + t9i23 * dvB) + 62.1 * exp(vC) * (-1.5 * t9i52 + t9i32 * dvC) +

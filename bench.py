@@ -54,6 +54,22 @@ def parse():
     return ap.parse_args()
 
 
+def shard_seed(rank):
+    """Seed of this rank's shard of the c2 workload (weak scaling: independent particles)."""
+    return 2 + 1000 * rank
+
+
+def max_over_ranks(ms, world, device="cpu"):
+    """Step time of the job: the maximum over ranks (the only collective of the bench)."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_info():
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
@@ -181,7 +197,7 @@ def main():
     sv = nn.SOLVERS[solver]
 
     # ---- device-resident workload (this rank's shard)
-    w = workloads.make("c2", P=args.particles, seed=2 + 1000 * rank)
+    w = workloads.make("c2", P=args.particles, seed=shard_seed(rank))
     P = args.particles
     Y0 = torch.tensor(w["Y"], device=dev)
     T0 = torch.tensor(w["T"], device=dev)
@@ -236,10 +252,7 @@ def main():
         wall = time.perf_counter() - t0
     ms = ev0.elapsed_time(ev1) / args.steps
     kernel_ms = statistics.mean(a.elapsed_time(b) for a, b in kt)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, world, dev)
     value = world * P / (ms / 1e3)
 
     # ---- end to end through the public API with host buffers

@@ -126,6 +126,8 @@ int uploadNetwork(int net, NetBuffer& b)
                  oSb = putv(sp.sbPos), oSbD = putv(sp.sbDiag);
     // warp-per-particle lists
     const WarpPlan wp = buildWarpPlan(sp, rbeg, rspec, rcnt, pbeg, pspec, pcnt, net == 14 ? kWarpNnzCap14 : kWarpNnzCap86);
+    if (wp.sgHeavy.size() > 8 || wp.jgHeavy.size() > 8 || wp.rjHeavy.size() > 8 || wp.rowHeavy.size() > 8)
+        return fail(NNET_ERR_TOO_LARGE, "network has more long gather lists than the warp kernels unroll");
     const size_t oSgC = putd(wp.sgCoef.data(), wp.sgCoef.size()), oJgC = putd(wp.jgCoef.data(), wp.jgCoef.size());
     const size_t oUpdB = putv(wp.updBeg), oUpdT = putv(wp.updT), oUpdL = putv(wp.updL), oUpdU = putv(wp.updU),
                  oUcB = putv(wp.ucBeg), oUcP = putv(wp.ucPos), oUcR = putv(wp.ucRow), oSgB = putv(wp.sgBeg),

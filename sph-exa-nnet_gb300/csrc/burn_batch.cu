@@ -532,7 +532,7 @@ __device__ void batchLoop(const BurnParams& bp, const NetView& nv, const HelmVie
 }
 
 template<int NET, int EOS, bool MIXED>
-__global__ void __launch_bounds__(64, 1) burnBatchKernel(BurnParams bp, NetView nv, HelmView hv, double* scratch,
+__global__ void __launch_bounds__(32, 9) burnBatchKernel(BurnParams bp, NetView nv, HelmView hv, double* scratch,
                                                       size_t /*unused*/)
 {
     extern __shared__ __align__(16) double smem[];
@@ -544,7 +544,7 @@ __global__ void __launch_bounds__(64, 1) burnBatchKernel(BurnParams bp, NetView 
 // drains the net86 queue, then net87, then net14, so the expensive particles start first and
 // the cheap ones fill the tail.  A warp changes network once all its lanes are idle.
 template<int EOS, bool MIXED>
-__global__ void __launch_bounds__(64, 1) burnBatchMultiKernel(MultiParams mp, HelmView hv, double* scratch,
+__global__ void __launch_bounds__(32, 9) burnBatchMultiKernel(MultiParams mp, HelmView hv, double* scratch,
                                                            size_t /*unused*/)
 {
     extern __shared__ __align__(16) double smem[];
@@ -561,8 +561,8 @@ template<int NET, int EOS, bool MIXED>
 KernelInfo batchInfo()
 {
     // lanesPerParticle = 32: a small batch is spread one particle per warp over the grid
-    return {(const void*)burnBatchKernel<NET, EOS, MIXED>, (size_t)2 * padN<NET>() + kSlotFields, 64,
-            WDims<NET>::NNZ, 2 * perWarpDoubles<NET, MIXED>() * sizeof(double), 32};
+    return {(const void*)burnBatchKernel<NET, EOS, MIXED>, (size_t)2 * padN<NET>() + kSlotFields, 32,
+            WDims<NET>::NNZ, perWarpDoubles<NET, MIXED>() * sizeof(double), 32};
 }
 
 template<int EOS, bool MIXED>
@@ -571,8 +571,8 @@ KernelInfo batchMultiInfo()
     static_assert(perWarpDoubles<87, MIXED>() >= perWarpDoubles<86, MIXED>() &&
                       perWarpDoubles<87, MIXED>() >= perWarpDoubles<14, MIXED>(),
                   "net87 has the largest warp layout");
-    return {(const void*)burnBatchMultiKernel<EOS, MIXED>, (size_t)2 * padN<87>() + kSlotFields, 64,
-            WDims<87>::NNZ, 2 * perWarpDoubles<87, MIXED>() * sizeof(double), 32};
+    return {(const void*)burnBatchMultiKernel<EOS, MIXED>, (size_t)2 * padN<87>() + kSlotFields, 32,
+            WDims<87>::NNZ, perWarpDoubles<87, MIXED>() * sizeof(double), 32};
 }
 
 template<bool MIXED>

@@ -18,6 +18,20 @@ __device__ __forceinline__ double warpSum(double v)
     return v;
 }
 
+// at most this many long (warp-split) lists per gather kind; checked when a network is uploaded
+constexpr int kMaxHeavy = 8;
+
+// warpSum of v[0..n) with the butterflies of the different sums interleaved (same order of
+// additions per sum as warpSum)
+__device__ __forceinline__ void warpSumMany(double (&v)[kMaxHeavy], int n)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int h = 0; h < kMaxHeavy; ++h)
+            if (h < n) v[h] += __shfl_xor_sync(kFull, v[h], o);
+}
+
 template<int NET>
 struct WDims
 {
@@ -110,18 +124,27 @@ __device__ void warpAssemble(const NetView& nv, WarpSmem<NET, MIXED>& S, double 
         }
         S.dYdt[s] = a, S.dYdT[s] = c;
     }
-    for (int h = 0; h < wv.nSgHeavy; ++h)
     {
-        const int s = __ldg(wv.sgHeavy + h), b0 = __ldg(wv.sgBeg + s), b1 = __ldg(wv.sgBeg + s + 1);
-        double    a = 0, c = 0;
-        for (int k = b0 + lane; k < b1; k += 32)
+        // the long lists: partial sums of all of them first, then their butterflies interleaved
+        double ha[kMaxHeavy], hc[kMaxHeavy];
+#pragma unroll
+        for (int h = 0; h < kMaxHeavy; ++h)
         {
-            const double w = __ldg(wv.sgCoef + k);
-            const int    r = __ldg(wv.sgRx + k);
-            a += w * S.f[r], c += w * S.df[r];
+            ha[h] = 0, hc[h] = 0;
+            if (h >= wv.nSgHeavy) continue;
+            const int s = __ldg(wv.sgHeavy + h), b0 = __ldg(wv.sgBeg + s), b1 = __ldg(wv.sgBeg + s + 1);
+            for (int k = b0 + lane; k < b1; k += 32)
+            {
+                const double w = __ldg(wv.sgCoef + k);
+                const int    r = __ldg(wv.sgRx + k);
+                ha[h] += w * S.f[r], hc[h] += w * S.df[r];
+            }
         }
-        a = warpSum(a), c = warpSum(c);
-        if (lane == 0) S.dYdt[s] = a, S.dYdT[s] = c;
+        warpSumMany(ha, wv.nSgHeavy), warpSumMany(hc, wv.nSgHeavy);
+        if (lane == 0)
+#pragma unroll
+            for (int h = 0; h < kMaxHeavy; ++h)
+                if (h < wv.nSgHeavy) S.dYdt[__ldg(wv.sgHeavy + h)] = ha[h], S.dYdT[__ldg(wv.sgHeavy + h)] = hc[h];
     }
     // Jacobian entries
     for (int m = lane; m < wv.nJ; m += 32)
@@ -133,14 +156,22 @@ __device__ void warpAssemble(const NetView& nv, WarpSmem<NET, MIXED>& S, double 
             a += __ldg(wv.jgCoef + k) * S.tr[__ldg(wv.jgEnt + k)];
         S.A[__ldg(wv.jPos + m)] = a;
     }
-    for (int h = 0; h < wv.nJgHeavy; ++h)
     {
-        const int m = __ldg(wv.jgHeavy + h), b0 = __ldg(wv.jgBeg + m), b1 = __ldg(wv.jgBeg + m + 1);
-        double    a = 0;
-        for (int k = b0 + lane; k < b1; k += 32)
-            a += __ldg(wv.jgCoef + k) * S.tr[__ldg(wv.jgEnt + k)];
-        a = warpSum(a);
-        if (lane == 0) S.A[__ldg(wv.jPos + m)] = a;
+        double ha[kMaxHeavy];
+#pragma unroll
+        for (int h = 0; h < kMaxHeavy; ++h)
+        {
+            ha[h] = 0;
+            if (h >= wv.nJgHeavy) continue;
+            const int m = __ldg(wv.jgHeavy + h), b0 = __ldg(wv.jgBeg + m), b1 = __ldg(wv.jgBeg + m + 1);
+            for (int k = b0 + lane; k < b1; k += 32)
+                ha[h] += __ldg(wv.jgCoef + k) * S.tr[__ldg(wv.jgEnt + k)];
+        }
+        warpSumMany(ha, wv.nJgHeavy);
+        if (lane == 0)
+#pragma unroll
+            for (int h = 0; h < kMaxHeavy; ++h)
+                if (h < wv.nJgHeavy) S.A[__ldg(wv.jPos + __ldg(wv.jgHeavy + h))] = ha[h];
     }
     __syncwarp();
     // J (Yg - Y) per species row (nuclear_net.hpp:580-589)
@@ -156,17 +187,25 @@ __device__ void warpAssemble(const NetView& nv, WarpSmem<NET, MIXED>& S, double 
         }
         S.jdy[i] = a;
     }
-    for (int h = 0; h < wv.nRjHeavy; ++h)
     {
-        const int i = __ldg(wv.rjHeavy + h), b0 = __ldg(wv.rjBeg + i), b1 = __ldg(wv.rjBeg + i + 1);
-        double    a = 0;
-        for (int k = b0 + lane; k < b1; k += 32)
+        double ha[kMaxHeavy];
+#pragma unroll
+        for (int h = 0; h < kMaxHeavy; ++h)
         {
-            const int m = __ldg(wv.rjEnt + k), j = __ldg(wv.jCol + m);
-            a += S.A[__ldg(wv.jPos + m)] * (S.Yn[j] - S.Y[j]);
+            ha[h] = 0;
+            if (h >= wv.nRjHeavy) continue;
+            const int i = __ldg(wv.rjHeavy + h), b0 = __ldg(wv.rjBeg + i), b1 = __ldg(wv.rjBeg + i + 1);
+            for (int k = b0 + lane; k < b1; k += 32)
+            {
+                const int m = __ldg(wv.rjEnt + k), j = __ldg(wv.jCol + m);
+                ha[h] += S.A[__ldg(wv.jPos + m)] * (S.Yn[j] - S.Y[j]);
+            }
         }
-        a = warpSum(a);
-        if (lane == 0) S.jdy[i] = a;
+        warpSumMany(ha, wv.nRjHeavy);
+        if (lane == 0)
+#pragma unroll
+            for (int h = 0; h < kMaxHeavy; ++h)
+                if (h < wv.nRjHeavy) S.jdy[__ldg(wv.rjHeavy + h)] = ha[h];
     }
     __syncwarp();
     // I - theta dt J, the temperature row / column and the right-hand side (:590-608)

@@ -489,9 +489,10 @@ def algorithmic_flops(nn, net, solver):
 
 
 FP64_PEAK_TFLOPS = 1.25
-# dram__bytes_read.sum + dram__bytes_write.sum of burnWarpKernel<86, Helmholtz> on 32,768 c2
-# particles (24.68 MB + 0.08 MB): the particle state, read once; tables stay in L2
-TRAFFIC_PER_PARTICLE = (24.677376e6 + 0.08192e6) / 32768
+# dram__bytes_read.sum + dram__bytes_write.sum of burnBatchKernel<86, Helmholtz> on 32,768 c2
+# particles (218.0 MB + 382.9 MB): the particle state, the batched slot scratch and register
+# spills of the scalar phase; tables stay in L2
+TRAFFIC_PER_PARTICLE = (218.009344e6 + 382.88e6) / 32768
 
 if __name__ == "__main__":
     main()

@@ -140,6 +140,7 @@ int uploadNetwork(int net, NetBuffer& b)
                  oTuL = putv(wp.tuL), oTuU = putv(wp.tuU), oFwB = putv(wp.fwBeg), oFwR = putv(wp.fwRow),
                  oFwE = putv(wp.fwEnt), oFlP = putv(wp.flPos), oFlK = putv(wp.flK), oBwB = putv(wp.bwBeg),
                  oBwR = putv(wp.bwRow), oBwE = putv(wp.bwEnt), oBuP = putv(wp.buPos), oBuK = putv(wp.buK);
+    const size_t oSgO = putv(wp.sgOrder), oRjO = putv(wp.rjOrder);
     const size_t oScB = putv(wp.scBeg), oScP = putv(wp.scPos), oScK = putv(wp.scPiv), oTgBA = putv(wp.tgBegA),
                  oTgPA = putv(wp.tgPosA), oTgUA = putv(wp.tgUpdA), oTuLA = putv(wp.tuLA), oTuUA = putv(wp.tuUA);
     const size_t bytesD = d.size() * sizeof(double), bytes = bytesD + ii.size() * sizeof(int);
@@ -175,6 +176,7 @@ int uploadNetwork(int net, NetBuffer& b)
     x.tgBeg = I + oTgB, x.tgPos = I + oTgP, x.tgUpd = I + oTgU, x.tuL = I + oTuL, x.tuU = I + oTuU;
     x.fwBeg = I + oFwB, x.fwRow = I + oFwR, x.fwEnt = I + oFwE, x.flPos = I + oFlP, x.flK = I + oFlK;
     x.bwBeg = I + oBwB, x.bwRow = I + oBwR, x.bwEnt = I + oBwE, x.buPos = I + oBuP, x.buK = I + oBuK;
+    x.sgOrder = I + oSgO, x.rjOrder = I + oRjO;
     x.rhsBase = wp.rhsBase;
     x.scBeg = I + oScB, x.scPos = I + oScP, x.scPiv = I + oScK, x.tgBegA = I + oTgBA, x.tgPosA = I + oTgPA;
     x.tgUpdA = I + oTgUA, x.tuLA = I + oTuLA, x.tuUA = I + oTuUA;

@@ -64,6 +64,7 @@ struct WarpView
     int        nLevels;
     const int *lvBeg, *lvPiv, *lsBeg, *lsPos, *lsPiv, *tgBeg, *tgPos, *tgUpd, *tuL, *tuU;
     const int *fwBeg, *fwRow, *fwEnt, *flPos, *flK, *bwBeg, *bwRow, *bwEnt, *buPos, *buK;
+    const int *sgOrder, *rjOrder;
     // fused forms (WarpPlan::scBeg ... tuUA)
     int        rhsBase;
     const int *scBeg, *scPos, *scPiv, *tgBegA, *tgPosA, *tgUpdA, *tuLA, *tuUA;

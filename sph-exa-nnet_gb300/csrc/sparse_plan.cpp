@@ -151,6 +151,20 @@ namespace nnet_gb300
 
 namespace
 {
+using Lists = std::map<int, std::vector<std::pair<int, int>>>;
+
+// A level's targets in the order the lanes take them: longest update lists first, so that
+// the 32 lanes of one round carry chains of similar length (ties by position).  The order
+// of the updates within a target is unchanged.
+std::vector<std::pair<int, const std::vector<std::pair<int, int>>*>> longestFirst(const Lists& m)
+{
+    std::vector<std::pair<int, const std::vector<std::pair<int, int>>*>> v;
+    for (auto& [t, lst] : m)
+        v.push_back({t, &lst});
+    std::stable_sort(v.begin(), v.end(), [](auto& a, auto& b) { return a.second->size() > b.second->size(); });
+    return v;
+}
+
 void buildLevels(const SparsePlan& P, WarpPlan& W, int rhsBase)
 {
     const int        n = P.n;
@@ -185,15 +199,17 @@ void buildLevels(const SparsePlan& P, WarpPlan& W, int rhsBase)
                     tgt[P.tPos[P.tBeg[e] + (u - P.uBeg[k])]].push_back({P.lPos[e], P.uPos[u]});
             }
         }
-        for (auto& [t, lst] : tgt)
+        for (auto& [t, lp] : longestFirst(tgt))
         {
+            auto& lst = *lp;
             W.tgPos.push_back(t);
             for (auto& pr : lst)
                 W.tuL.push_back(pr.first), W.tuU.push_back(pr.second);
             W.tgUpd.push_back((int)W.tuL.size());
         }
-        for (auto& [r, lst] : fw)
+        for (auto& [r, lp] : longestFirst(fw))
         {
+            auto& lst = *lp;
             W.fwRow.push_back(r);
             for (auto& pr : lst)
                 W.flPos.push_back(pr.first), W.flK.push_back(pr.second);
@@ -221,8 +237,9 @@ void buildLevels(const SparsePlan& P, WarpPlan& W, int rhsBase)
                 tgt[rhsBase + P.lRow[e]].push_back({P.lPos[e], rhsBase + k});
             }
         }
-        for (auto& [t, lst] : tgt)
+        for (auto& [t, lp] : longestFirst(tgt))
         {
+            auto& lst = *lp;
             W.tgPosA.push_back(t);
             for (auto& pr : lst)
                 W.tuLA.push_back(pr.first), W.tuUA.push_back(pr.second);
@@ -239,8 +256,9 @@ void buildLevels(const SparsePlan& P, WarpPlan& W, int rhsBase)
         for (int k : piv[l])
             for (int q = W.ucBeg[k]; q < W.ucBeg[k + 1]; ++q)
                 bw[W.ucRow[q]].push_back({W.ucPos[q], k});
-        for (auto& [r, lst] : bw)
+        for (auto& [r, lp] : longestFirst(bw))
         {
+            auto& lst = *lp;
             W.bwRow.push_back(r);
             for (auto& pr : lst)
                 W.buPos.push_back(pr.first), W.buK.push_back(pr.second);
@@ -315,6 +333,18 @@ WarpPlan buildWarpPlan(const SparsePlan& P, const int* rbeg, const int* rspec, c
             }
             jg[entryOf[pos]].push_back({e, P.cCoef[c]});
         }
+    // entries with the longest contribution lists first (balanced rounds of the warp)
+    {
+        std::vector<int> ord(jg.size());
+        for (size_t m = 0; m < ord.size(); ++m)
+            ord[m] = (int)m;
+        std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return jg[a].size() > jg[b].size(); });
+        std::vector<int> jp, jr, jc;
+        std::vector<std::vector<std::pair<int, double>>> jgs;
+        for (int m : ord)
+            jp.push_back(W.jPos[m]), jr.push_back(W.jRow[m]), jc.push_back(W.jCol[m]), jgs.push_back(jg[m]);
+        W.jPos = jp, W.jRow = jr, W.jCol = jc, jg = jgs;
+    }
     W.jgBeg.push_back(0);
     for (auto& l : jg)
     {
@@ -333,6 +363,13 @@ WarpPlan buildWarpPlan(const SparsePlan& P, const int* rbeg, const int* rspec, c
             W.rjEnt.push_back(m);
         W.rjBeg.push_back((int)W.rjEnt.size());
     }
+    // species and J-row gathers in the order the lanes take them: longest lists first
+    for (int i = 0; i < N; ++i)
+        W.sgOrder.push_back(i), W.rjOrder.push_back(i);
+    std::stable_sort(W.sgOrder.begin(), W.sgOrder.end(),
+                     [&](int a, int b) { return W.sgBeg[a + 1] - W.sgBeg[a] > W.sgBeg[b + 1] - W.sgBeg[b]; });
+    std::stable_sort(W.rjOrder.begin(), W.rjOrder.end(),
+                     [&](int a, int b) { return W.rjBeg[a + 1] - W.rjBeg[a] > W.rjBeg[b + 1] - W.rjBeg[b]; });
     W.entRx.assign(rbeg[R], 0);
     for (int r = 0; r < R; ++r)
         for (int k = rbeg[r]; k < rbeg[r + 1]; ++k)

@@ -67,6 +67,8 @@ struct WarpPlan
     std::vector<int> rjBeg, rjEnt;
     // reaction of every reactant entry
     std::vector<int> entRx;
+    // species (dY/dt) and J rows (J (Yn - Y)) in the order the lanes take them
+    std::vector<int> sgOrder, rjOrder;
     // targets whose lists are longer than kHeavy (summed by the whole warp)
     std::vector<int> sgHeavy, jgHeavy, rjHeavy, rowHeavy; // species, J entries, J rows, factor rows
 

@@ -111,9 +111,9 @@ __device__ void warpAssemble(const NetView& nv, WarpSmem<NET, MIXED>& S, double 
         S.A[p] = 0.;
     __syncwarp();
     // dY/dt and d(dY/dt)/dT per species
-    for (int s = lane; s < D::N; s += 32)
+    for (int t = lane; t < D::N; t += 32)
     {
-        const int b0 = __ldg(wv.sgBeg + s), b1 = __ldg(wv.sgBeg + s + 1);
+        const int s = __ldg(wv.sgOrder + t), b0 = __ldg(wv.sgBeg + s), b1 = __ldg(wv.sgBeg + s + 1);
         if (b1 - b0 > WarpPlan::kHeavy) continue;
         double a = 0, c = 0;
         for (int k = b0; k < b1; ++k)
@@ -175,9 +175,9 @@ __device__ void warpAssemble(const NetView& nv, WarpSmem<NET, MIXED>& S, double 
     }
     __syncwarp();
     // J (Yg - Y) per species row (nuclear_net.hpp:580-589)
-    for (int i = lane; i < D::N; i += 32)
+    for (int t = lane; t < D::N; t += 32)
     {
-        const int b0 = __ldg(wv.rjBeg + i), b1 = __ldg(wv.rjBeg + i + 1);
+        const int i = __ldg(wv.rjOrder + t), b0 = __ldg(wv.rjBeg + i), b1 = __ldg(wv.rjBeg + i + 1);
         if (b1 - b0 > WarpPlan::kHeavy) continue;
         double a = 0;
         for (int k = b0; k < b1; ++k)

@@ -577,7 +577,10 @@ extern "C" int nnet_burn_batch(nnet_handle h, const nnet_burn_args* batches, int
     if (total == 0) return NNET_SUCCESS;
     NNET_CUDA(cudaSetDevice(h->device));
     cudaStream_t st = (cudaStream_t)stream;
-    const bool   tpp = batches[0].solver == NNET_SOLVER_DENSE_FP64 || h->layout == NNET_LAYOUT_THREAD;
+    // thread layout: dense and sparse FP64 only (its mixed-precision multi-network form
+    // disagreed with the per-network burns on a few percent of c3 particles, cause not found)
+    const bool   tpp = batches[0].solver == NNET_SOLVER_DENSE_FP64 ||
+                     (h->layout == NNET_LAYOUT_THREAD && batches[0].solver == NNET_SOLVER_SPARSE_FP64);
     KernelInfo   ki  = tpp ? multiKernel(batches[0].eos, batches[0].solver)
                            : batchMultiKernel(batches[0].eos, batches[0].solver == NNET_SOLVER_MIXED);
     for (int ni = 0; ni < 3; ++ni)

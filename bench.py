@@ -11,7 +11,9 @@ carried through one hydro step per second of wall time).
                   [--particles P] [--impl reference]
 
 Under torchrun each rank burns its own seeded shard of P particles (weak scaling, no
-collective on the data path); the step time is the max over ranks.
+collective on the data path); the step time is the max over ranks.  --strong splits one set
+of P particles over the ranks in contiguous ranges of equal predicted cost (the previous
+burn's Newton iterations per particle, exchanged once on the host).
 """
 import argparse
 import json
@@ -51,6 +53,11 @@ def parse():
     ap.add_argument("--no-graph", action="store_true", help="launch the timed steps eagerly")
     ap.add_argument("--workload", default="c2",
                     help="c2 (default line), or c1 / c3 / c4 for the other configurations (one GPU)")
+    ap.add_argument("--no-mixed-leg", action="store_true", help="skip the FP32-LU (mixed) leg of the c2 line")
+    ap.add_argument("--no-fused-leg", action="store_true", help="skip the fused post-burn EOS leg of the c2 line")
+    ap.add_argument("--strong", action="store_true",
+                    help="N > 1: split ONE set of --particles particles over the ranks by cost-balanced contiguous "
+                         "ranges (strong scaling) instead of one shard of --particles per rank (weak scaling)")
     return ap.parse_args()
 
 
@@ -126,49 +133,78 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------- reference (CPU) arm
-def cpu_burn_rate(sample, threads=0, seed=None):
-    """The oracle restatement of the reference's CPU path on host cores (OpenMP dynamic
-    schedule, as parallel_nuclear_net_impl.cpp:79-81) over `sample` particles of the
-    workload; returns (particle-burns/s, seconds, threads)."""
+def _oracle():
+    """The oracle restatement of the reference's CPU path, built with the compiler line
+    oracle/build.py reports (test infrastructure: used only as the timed baseline and checker)."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import importlib.util
     spec = importlib.util.spec_from_file_location("oracle_build", os.path.join(REPO, "oracle", "build.py"))
     ob = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(ob)
     ob.build_oracle()
-    from oracle import Oracle
-    import workloads
+    import oracle
     import nnet_build
-    o = Oracle("port")
+    o = oracle.Oracle("port")
     o.load_helmholtz(np.fromfile(nnet_build.helm_table(), dtype="<f8"))
-    w = workloads.make("c2", P=sample, seed=seed)
+    return o, oracle, ob.CPU_FLAGS
+
+
+def status_summary(status, substeps, iterations, seconds):
+    """Counts per status, throughput over completed (OK) particles, and p50 / p99 of the
+    substeps and Newton iterations per particle."""
+    names = ["OK", "SKIPPED", "LIVELOCK", "MAXITER", "ZERO_DT", "ABORTED"]
+    counts = np.bincount(np.asarray(status, dtype=np.int64), minlength=len(names))
+    it, sub = np.asarray(iterations), np.asarray(substeps)
+    return {"status_counts": dict(zip(names, [int(c) for c in counts])),
+            "completed_value": float(counts[0] / seconds),
+            "substeps_p50": float(np.percentile(sub, 50)), "substeps_p99": float(np.percentile(sub, 99)),
+            "iterations_p50": float(np.percentile(it, 50)), "iterations_p99": float(np.percentile(it, 99)),
+            "iterations_max": int(it.max()) if it.size else 0}
+
+
+def cpu_burn(o, w, sl, threads=0):
+    """Burn particles `sl` of workload `w` with the oracle on the host cores (OpenMP dynamic
+    schedule, as parallel_nuclear_net_impl.cpp:79-81); returns (seconds, threads, outputs)."""
     threads = threads or os.cpu_count()
     t0 = time.perf_counter()
-    o.burn(w["net"], w["Y"], w["T"], w["rho"], w["dt"], w["hydro_dt"], w["eos"], w["mu"], max_iter=20000,
-           nthreads=threads)
-    el = time.perf_counter() - t0
-    return sample / el, el, threads
+    out = o.burn(w["net"], w["Y"][:, sl], w["T"][sl], w["rho"][sl], w["dt"][sl], w["hydro_dt"], w["eos"], w["mu"],
+                 max_iter=20000, nthreads=threads)
+    return time.perf_counter() - t0, threads, out
 
 
 def run_reference(args):
+    """The reference's CPU path (the oracle restatement, bit-identical to the reference compiled
+    from its sources) on the machine's host cores: step k burns particles [k S, (k + 1) S) of the
+    timed c2 set (S = --cpu-sample), so the steps walk through the particles the GPU arm burns."""
     rank, world, _ = dist_info()
     if rank != 0:
         return
-    vals = []
-    for _ in range(max(1, args.warmup // 3)):
-        cpu_burn_rate(256)
+    import workloads
+    o, _, flags = _oracle()
+    w = workloads.make("c2", P=args.particles, seed=shard_seed(0))
+    S = min(args.cpu_sample, args.particles)
+    nslices = max(1, args.particles // S)
+    cpu_burn(o, w, slice(0, 256))  # warm-up (thread pool, page-in)
+    vals, outs = [], []
     for k in range(args.steps):
-        v, el, threads = cpu_burn_rate(args.cpu_sample, seed=100 + k)
-        vals.append((v, el))
-    value = statistics.median(v for v, _ in vals)
+        a = (k % nslices) * S
+        el, threads, out = cpu_burn(o, w, slice(a, a + S))
+        vals.append(el)
+        outs.append(out)
+    value = statistics.median(S / e for e in vals)
+    st = np.concatenate([x[3] for x in outs])
+    summ = status_summary(st, np.concatenate([x[4] for x in outs]), np.concatenate([x[5] for x in outs]), sum(vals))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.median(e for _, e in vals) * 1e3,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.median(vals) * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded, workload c2 distributions)",
-            "config": {"workload": "net86+helmholtz c2 (CPU sample)", "particles_per_step": args.cpu_sample,
-                       "hydro_dt": 1e-4},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"{args.cpu_sample} particles of c2 per step (fresh seed each step)"},
+            "config": {"workload": "net86+helmholtz c2 (CPU sample)", "particles_per_step": S, "hydro_dt": 1e-4,
+                       "value_counts": "every particle carried through the call (any final status); "
+                                       "completed_value counts status OK only",
+                       **{k: v for k, v in summ.items() if k != "completed_value"}},
+            "completed_value": summ["completed_value"],
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "build": flags,
+                             "sample": f"step k: particles [k*{S}, (k+1)*{S}) of the timed c2 set"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -197,20 +233,30 @@ def main():
     sv = nn.SOLVERS[solver]
 
     # ---- device-resident workload (this rank's shard)
-    w = workloads.make("c2", P=args.particles, seed=shard_seed(rank))
-    P = args.particles
+    partition = None
+    if args.strong and world > 1:
+        w, partition = strong_shard(args, ctx, rank, world, dev)
+    else:
+        w = workloads.make("c2", P=args.particles, seed=shard_seed(rank))
+    P = w["T"].size
+    P_job = args.particles if partition else world * P
     Y0 = torch.tensor(w["Y"], device=dev)
     T0 = torch.tensor(w["T"], device=dev)
     rho = torch.tensor(w["rho"], device=dev)
     dt0 = torch.tensor(w["dt"], device=dev)
     Y, T, dt = torch.empty_like(Y0), torch.empty_like(T0), torch.empty_like(dt0)
     status = torch.empty(P, dtype=torch.int32, device=dev)
+    substeps = torch.empty(P, dtype=torch.int32, device=dev)
+    iterations = torch.empty(P, dtype=torch.int32, device=dev)
     stream = torch.cuda.current_stream(dev)
 
-    def step(st=None):
+    def restore():
         Y.copy_(Y0), T.copy_(T0), dt.copy_(dt0)
-        ctx.burn(86, Y, T, rho, dt, w["hydro_dt"], eos=nn.EOS_HELMHOLTZ, solver=sv, status=status,
-                 max_iter=args.max_iter, stream=st or stream)
+
+    def step(st=None, sv_=sv, **kw):
+        restore()
+        ctx.burn(86, Y, T, rho, dt, w["hydro_dt"], eos=nn.EOS_HELMHOLTZ, solver=sv_, status=status,
+                 substeps=substeps, iterations=iterations, max_iter=args.max_iter, stream=st or stream, **kw)
 
     def barrier():
         torch.cuda.synchronize(dev)
@@ -253,7 +299,11 @@ def main():
     ms = ev0.elapsed_time(ev1) / args.steps
     kernel_ms = statistics.mean(a.elapsed_time(b) for a, b in kt)
     ms = max_over_ranks(ms, world, dev)
-    value = world * P / (ms / 1e3)
+    value = P_job / (ms / 1e3)
+    # every timed step burns the same state: the last one's per-particle results
+    S = min(args.cpu_sample, P)
+    res_fast = (Y[:, :S].cpu().numpy(), T[:S].cpu().numpy(), dt[:S].cpu().numpy(), status[:S].cpu().numpy())
+    summ = status_summary(status.cpu().numpy(), substeps.cpu().numpy(), iterations.cpu().numpy(), ms / 1e3)
 
     # ---- end to end through the public API with host buffers
     Yh = torch.tensor(w["Y"]).pin_memory()
@@ -277,6 +327,56 @@ def main():
     e2e_ms = e0.elapsed_time(e1) / e2e_steps
     h2d = (86 + 3) * 8 * P
     d2h = (86 + 2) * 8 * P
+
+    # ---- the mixed-precision form (FP32 LU, FP64 residual refinement) on the same particles
+    mixed = None
+    if not args.no_mixed_leg and solver != "mixed" and rank == 0:
+        step(sv_=nn.SOLVER_MIXED)  # warm-up: module load
+        barrier()
+        m0, m1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        restore()
+        m0.record(stream)
+        ctx.burn(86, Y, T, rho, dt, w["hydro_dt"], eos=nn.EOS_HELMHOLTZ, solver=nn.SOLVER_MIXED, status=status,
+                 substeps=substeps, iterations=iterations, max_iter=args.max_iter, stream=stream)
+        m1.record(stream)
+        barrier()
+        mms = m0.elapsed_time(m1)
+        mst = ctx.stats()
+        res_mixed = (Y[:, :S].cpu().numpy(), T[:S].cpu().numpy(), dt[:S].cpu().numpy(), status[:S].cpu().numpy())
+        mixed = {"value": P / (mms / 1e3), "unit": UNIT, "ms_per_step": mms, "steps": 1,
+                 "newton_iterations": mst["newton_iterations"], "refinement_steps": mst["refinement_steps"],
+                 "fp64_fallbacks": mst["fp64_fallbacks"],
+                 "fp64_fallback_frac": mst["fp64_fallbacks"] / max(1, mst["newton_iterations"]),
+                 **status_summary(status.cpu().numpy(), substeps.cpu().numpy(), iterations.cpu().numpy(), mms / 1e3)}
+
+    # ---- post-burn steps fused into the burn (normalisation + drift + Helmholtz EOS) against
+    #      the burn followed by the stand-alone EOS kernel (nnet_helmholtz_eos)
+    fused = None
+    if not args.no_fused_leg and rank == 0:
+        outs = [torch.empty(P, dtype=torch.float64, device=dev) for _ in range(5)]
+        drift = torch.empty(P, dtype=torch.float64, device=dev)
+        Z = nn.network_charges(86)
+        q = slice(0, 1024)
+        Y[:, q].copy_(Y0[:, q]), T[q].copy_(T0[q]), dt[q].copy_(dt0[q])
+        ctx.burn(86, Y[:, q], T[q], rho[q], dt[q], w["hydro_dt"], eos=nn.EOS_HELMHOLTZ, solver=sv,
+                 max_iter=args.max_iter, normalize_mass=True, mass_drift=drift[q], eos_out=[o[q] for o in outs],
+                 stream=stream)  # warm-up: module load
+        ctx.helmholtz_eos(Z, T, rho, Y, *outs, stream=stream)
+        barrier()
+        f0, f1, f2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        restore()
+        f0.record(stream)
+        ctx.burn(86, Y, T, rho, dt, w["hydro_dt"], eos=nn.EOS_HELMHOLTZ, solver=sv, max_iter=args.max_iter,
+                 normalize_mass=True, mass_drift=drift, eos_out=outs, stream=stream)
+        f1.record(stream)
+        ctx.helmholtz_eos(Z, T, rho, Y, *outs, stream=stream)  # the separate pass, on the same state
+        f2.record(stream)
+        barrier()
+        A = torch.tensor(workloads.mass_numbers(86)[:86], dtype=torch.float64, device=dev)[:, None]
+        sum_err = ((A * Y).sum(0) - 1).abs().max().item()
+        fused = {"fused_ms": f0.elapsed_time(f1), "separate_eos_ms": f1.elapsed_time(f2),
+                 "burn_then_eos_ms": kernel_ms + f1.elapsed_time(f2),
+                 "max_abs_sum_x_minus_1_after": sum_err, "max_abs_drift_before": drift.abs().max().item()}
 
     # ---- plain FP64 form on a sub-batch, for the plain-vs-fast ratio
     plain = None
@@ -314,13 +414,19 @@ def main():
     except Exception:
         peak, peak_src = FP64_PEAK_TFLOPS, "nominal GB300 FP64 (probe failed)"
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "strong" if partition else "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, workload c2 distributions)",
-            "config": {"workload": "net86+helmholtz c2", "particles_per_gpu": P, "hydro_dt": 1e-4,
+            "config": {"workload": "net86+helmholtz c2", "particles_per_gpu": P, "particles_job": P_job,
+                       "partition": partition, "hydro_dt": 1e-4,
                        "solver": solver, "l2": "inputs (700 MB of abundances) larger than L2",
                        "launch": launch, "layout": "batched (32 particles per warp)",
-                       "newton_iterations_per_step": iters, "status_counts": stats["status"]},
-            "e2e": {"value": world * P / (e2e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                       "value_counts": "every particle carried through the call (any final status); "
+                                       "completed_value counts status OK only",
+                       "newton_iterations_per_step": iters,
+                       **{k: v for k, v in summ.items() if k != "completed_value"}},
+            "completed_value": summ["completed_value"] * P_job / P,
+            "e2e": {"value": P_job / (e2e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": args.steps,
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
@@ -331,6 +437,10 @@ def main():
                          "flops_per_newton_iteration": flops_per_iter,
                          "refinement_steps": stats["refinement_steps"], "fp64_fallbacks": stats["fp64_fallbacks"]},
             "kernel_ms": kernel_ms, "wall_s": wall, "clocks": clk.summary()}
+    if mixed:
+        line["mixed_fp32lu"] = mixed
+    if fused:
+        line["post_burn_fused"] = fused
     if plain:
         line["plain_fp64"] = plain
     if args.serve_requests and rank == 0:
@@ -342,16 +452,57 @@ def main():
                 "fast": serve_bench(nn, ctx, solver, args.serve_plain_requests, 6, scale=128),
                 "plain_fp64": serve_bench(nn, ctx, "dense", args.serve_plain_requests, 6, scale=128)}
     if rank == 0:
+        # the reference's CPU path on the first S particles of the timed set: timed as the
+        # baseline, and the checker of the GPU results of those particles
         try:
-            v, el, thr = cpu_burn_rate(args.cpu_sample)
-            line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": thr, "kind": "port",
-                                    "sample": f"{args.cpu_sample} particles of c2, {el:.1f} s"}
+            o, oracle, flags = _oracle()
+            el, thr, out = cpu_burn(o, w, slice(0, S))
+            line["cpu_baseline"] = {"value": S / el, "unit": UNIT, "cores": thr, "kind": "port", "build": flags,
+                                    "sample": f"particles [0, {S}) of the timed c2 set, {el:.1f} s",
+                                    "completed_value": float((out[3] == 0).sum() / el)}
+            Ys = w["Y"][:, :S]
+            line["parity"] = {"vs": "oracle (the reference's CPU path restated, bit-identical to the reference "
+                                    f"built from its sources) on particles [0, {S}) of the timed set",
+                              solver: oracle.compare_burns(86, Ys, res_fast, out)}
+            if mixed:
+                line["parity"]["mixed"] = oracle.compare_burns(86, Ys, res_mixed, out)
         except Exception as e:  # the baseline is reported, never the target
             line["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "error": str(e)}
         print(json.dumps(line), flush=True)
     ctx.close()
     if world > 1:
         dist.destroy_process_group()
+
+
+def strong_shard(args, ctx, rank, world, dev):
+    """Strong scaling: this rank's contiguous range of ONE c2 set, balanced on predicted cost.
+    A first (untimed) burn of equal-count ranges gives each particle's Newton iterations; the
+    ranks exchange them on the host (the only exchange: particles never move between steps) and
+    cut the set with sharding.partition.  Returns (this rank's workload slice, the ranges)."""
+    import torch
+    import torch.distributed as dist
+    import nnet_gb300 as nn
+    import sharding
+    import workloads
+    w = workloads.make("c2", P=args.particles, seed=shard_seed(0))
+    P = args.particles
+
+    def piece(a, b):
+        return dict(w, Y=w["Y"][:, a:b], T=w["T"][a:b], rho=w["rho"][a:b], dt=w["dt"][a:b])
+
+    a, b = rank * P // world, (rank + 1) * P // world
+    q = piece(a, b)
+    Y, T = torch.tensor(q["Y"], device=dev), torch.tensor(q["T"], device=dev)
+    rho, dt = torch.tensor(q["rho"], device=dev), torch.tensor(q["dt"], device=dev)
+    it = torch.zeros(b - a, dtype=torch.int32, device=dev)
+    ctx.burn(86, Y, T, rho, dt, w["hydro_dt"], eos=nn.EOS_HELMHOLTZ, solver=args.solver or "sparse",
+             iterations=it, max_iter=args.max_iter)
+    torch.cuda.synchronize(dev)
+    parts = [None] * world
+    dist.all_gather_object(parts, it.cpu().numpy())
+    ranges = sharding.partition(sharding.cost_estimate(prev_iterations=np.concatenate(parts)), world)
+    a, b = ranges[rank]
+    return piece(a, b), ranges
 
 
 # ---------------------------------------------------------------- other configurations

@@ -41,6 +41,7 @@ enum nnet_error
     NNET_ERR_NO_TABLE    = -3, /* Helmholtz EOS requested before a table was loaded */
     NNET_ERR_TOO_LARGE   = -4, /* request exceeds a fixed capacity */
     NNET_ERR_FILE        = -5, /* table file missing or malformed */
+    NNET_ERR_ABORTED     = -6, /* nnet_get_stats: the last launch hit its time limit (time_limit_seconds) */
 };
 
 /* Per-particle outcome written to nnet_burn_args.status (int32 per particle). */
@@ -54,6 +55,11 @@ enum nnet_particle_status
                                    with :899-904); Y and T are those of the last accepted substep */
     NNET_PARTICLE_MAXITER  = 3, /* Newton-iteration budget exhausted */
     NNET_PARTICLE_ZERO_DT  = 4, /* timestep underflowed to 0 (the reference throws, nuclear_net.hpp:533-549) */
+    NNET_PARTICLE_ABORTED  = 5, /* the launch reached nnet_burn_args.time_limit_seconds (no reference
+                                   counterpart): a particle in progress keeps its last accepted substep
+                                   (Y, T) and its current timestep proposal; a particle not yet started
+                                   keeps its input state */
+    NNET_NUM_PARTICLE_STATUS = 6
 };
 
 enum nnet_network
@@ -73,7 +79,7 @@ enum nnet_eos
 enum nnet_solver
 {
     NNET_SOLVER_DENSE_FP64  = 0, /* plain form: dense Gaussian elimination in the reference's
-                                    operation order (eigen.hpp:155-198), one thread per particle */
+                                    operation order (eigen.hpp:178-223), one thread per particle */
     NNET_SOLVER_SPARSE_FP64 = 1, /* fill-reducing sparse LU in FP64 */
     NNET_SOLVER_MIXED       = 2, /* sparse LU factored in FP32, FP64 residual, iterative refinement */
 };
@@ -96,7 +102,7 @@ typedef struct
 {
     unsigned long long newton_iterations;
     unsigned long long substeps;
-    unsigned long long status_count[5]; /* indexed by nnet_particle_status */
+    unsigned long long status_count[NNET_NUM_PARTICLE_STATUS]; /* indexed by nnet_particle_status */
     unsigned long long refinement_steps; /* NNET_SOLVER_MIXED: FP64-residual refinement steps */
     unsigned long long fp64_fallbacks;   /* NNET_SOLVER_MIXED: systems re-solved in FP64 */
 } nnet_stats;
@@ -123,6 +129,35 @@ typedef struct
     int32_t*      status;       /* optional, nnet_particle_status per particle */
     int32_t*      substeps;     /* optional, accepted substeps per particle */
     int32_t*      iterations;   /* optional, Newton iterations per particle */
+
+    /* Launch watchdog (no reference counterpart).  > 0: after this many seconds of GPU time the
+     * launch takes no further Newton iteration; unfinished particles end with
+     * NNET_PARTICLE_ABORTED and nnet_get_stats returns NNET_ERR_ABORTED.  <= 0: no limit. */
+    double        time_limit_seconds;
+
+    /* Post-burn steps, applied after each particle's burn (no reference counterpart unless noted).
+     * The reference only clips abundances at 1e-16 (nuclear_net.hpp:760) and accepts a substep
+     * after 11 Newton iterations whether or not the abundances converged (:763-764), so
+     * sum_i X_i drifts from 1; these steps report and remove the drift. */
+    int           normalize_mass; /* nonzero: Y_i <- Y_i / sum_j A_j Y_j for every particle not
+                                     skipped, so sum_i X_i = 1 to rounding (X_i = A_i Y_i; the net87
+                                     electron entry has A = 0) */
+    double*       mass_drift;     /* optional, per particle: sum_i A_i Y_i - 1 of the burned state,
+                                     before normalisation (skipped particles: of their input state) */
+    /* optional, all five or none: the post-burn Helmholtz EOS at the final (Y, T, rho) of every
+     * particle, over the network's charges (computeHelmEOS, parallel_nuclear_net.hpp:191-261; needs
+     * a loaded table).  The batched layout evaluates it as each particle retires; the other layouts
+     * in one pass after the burn. */
+    double*       u;
+    double*       cv;
+    double*       p;
+    double*       c;
+    double*       dpdT;
+
+    /* Optional device array of num_particles particle indices, a permutation (no reference
+     * counterpart): the work queue hands out particle order[k] k-th.  Per-particle results do
+     * not depend on it; only the launch's schedule does.  NULL: index order. */
+    const uint32_t* order;
 } nnet_burn_args;
 
 /* Create a context on `device` (network tables uploaded, no Helmholtz table yet). */
@@ -135,8 +170,9 @@ int nnet_destroy(nnet_handle h);
  * dpdfdt ef efd eft efdt xf xfd xft xfdt, each row-major [density][temperature].
  * Synchronous.  Replaces readCPUTable + copyTableToGPU (helmholtz.cpp:89-218). */
 int nnet_load_helmholtz_table(nnet_handle h, const double* table);
-/* Same, parsing the reference's text layout helm_table.dat (helmholtz.cpp:100-137); an
- * optional STR( ... ) wrapper is accepted. */
+/* Same, from a file: the reference's text layout helm_table.dat (helmholtz.cpp:100-137, an
+ * optional STR( ... ) wrapper is accepted), or the 21 x 541 x 201 little-endian doubles of
+ * nnet_load_helmholtz_table written as raw bytes. */
 int nnet_load_helmholtz_table_file(nnet_handle h, const char* path);
 
 /* Burn num_particles particles over hydro_dt on `stream` (a cudaStream_t, 0 = legacy
@@ -149,7 +185,8 @@ int nnet_burn(nnet_handle h, const nnet_burn_args* args, void* stream);
  * first.  Same semantics and, per layout, the same results per particle as nnet_burn. */
 int nnet_burn_batch(nnet_handle h, const nnet_burn_args* batches, int count, void* stream);
 /* Copy the statistics of the last nnet_burn issued on this handle (synchronises the
- * handle's internal stream). */
+ * stream of that call).  Returns NNET_ERR_ABORTED, with the statistics filled in, when that
+ * launch stopped at its time limit. */
 int nnet_get_stats(nnet_handle h, nnet_stats* out);
 
 /* Post-burn Helmholtz EOS over a batch (computeHelmEOS, parallel_nuclear_net.hpp:191-231):
@@ -225,10 +262,17 @@ int nnet_measure_fp64_peak(int device, double* tflops);
  * and results as nnet_burn with the batched layout; sparse and mixed solvers only.  Allocates
  * nothing: its slot scratch (7.2 MiB, 4096 particle slots) and counters are fixed arrays that
  * every GPU loading the library holds until exit; the grid is capped to them, so any number of
- * particles is accepted.  The first call on a device looks the arrays up (make it before any
- * stream capture).  Calls share the arrays: calls that overlap on the GPU race, and
- * nnet_get_stats does not report these calls. */
+ * particles is accepted.  The first call on a handle looks the arrays' device addresses up and
+ * keeps them in the handle (make it before any stream capture).  Calls share the arrays: calls
+ * that overlap on the GPU race, and nnet_get_stats does not report these calls. */
 int nnet_burn_noalloc(nnet_handle h, const nnet_burn_args* args, void* stream);
+
+/* Visiting order for nnet_burn_args.order with the costliest particles first (no reference
+ * counterpart): a permutation of [0, num_particles) sorted by decreasing floor(log2(cost[i]))
+ * (costs <= 1 last), from device arrays `cost` (int32, e.g. the previous burn's iterations)
+ * into `order` (uint32).  Asynchronous on `stream`; the order within a power-of-two cost class is
+ * unspecified.  The first call on a handle allocates 512 bytes of counters. */
+int nnet_cost_order(nnet_handle h, size_t num_particles, const int32_t* cost, uint32_t* order, void* stream);
 
 /* Batched layout: particles in flight per warp, 1..32 (default 32; no reference counterpart,
  * chosen by the autotuner).  Fewer slots shorten each particle's time per Newton iteration

@@ -14,6 +14,7 @@
 // any vector whose data() yields a raw device pointer are accepted.
 #pragma once
 
+#include <cstdlib>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -94,18 +95,38 @@ void eosArgs(const IdealGasFunctor<Float>& e, nnet_burn_args& a)
 }
 } // namespace detail
 
-// Process-wide context on the current device (tables loaded once, as the reference's
-// static-initialisation table reads).
+// Process-wide context (tables loaded once, as the reference's static-initialisation table
+// reads, helmholtz.cpp:89-218).  The Helmholtz table comes from, in order: `helmTable`, the
+// compile-time path NNET_GB300_HELM_TABLE (the reference compiles its table path in the same
+// way, HELM_TABLE_PATH), or the environment variable NNET_HELM_TABLE; either file layout of
+// nnet_load_helmholtz_table_file.  Without one, burns with HelmholtzFunctor throw, naming
+// these three ways.  The first call fixes the device and the table.
 inline nnet_handle defaultContext(int device = 0, const char* helmTable = nullptr)
 {
     static nnet_handle h = nullptr;
     if (!h)
     {
         detail::check(nnet_create(device, &h));
+#ifdef NNET_GB300_HELM_TABLE
+        if (!helmTable) helmTable = NNET_GB300_HELM_TABLE;
+#endif
+        if (!helmTable) helmTable = std::getenv("NNET_HELM_TABLE");
         if (helmTable) detail::check(nnet_load_helmholtz_table_file(h, helmTable));
     }
     return h;
 }
+
+namespace detail
+{
+inline void checkBurn(int rc)
+{
+    if (rc == NNET_ERR_NO_TABLE)
+        throw std::runtime_error("nnet_gb300: the Helmholtz EOS needs a table: pass its path to "
+                                 "nnet_gb300::defaultContext(device, path) before the first burn, compile with "
+                                 "-DNNET_GB300_HELM_TABLE=\"path\", or set NNET_HELM_TABLE");
+    check(rc);
+}
+} // namespace detail
 
 namespace parallel
 {
@@ -139,7 +160,7 @@ void computeNuclearReactions(Data& n, size_t firstIndex, size_t lastIndex, const
     a.previous_dt   = previous_dt;
     a.use_drhodt    = use_drhodt;
     nnet_handle ctx = h ? h : defaultContext();
-    detail::check(nnet_burn(ctx, &a, nullptr));
+    detail::checkBurn(nnet_burn(ctx, &a, nullptr));
     nnet_stats st;
     detail::check(nnet_get_stats(ctx, &st)); // synchronises, as the reference's blocking call
 }
@@ -155,7 +176,7 @@ void computeHelmEOS(Data& n, size_t firstIndex, size_t lastIndex, const Vector& 
     for (int j = 0; j < dim; ++j)
         Y[j] = detail::raw(d.Y[j], firstIndex);
     nnet_handle ctx = h ? h : defaultContext();
-    detail::check(nnet_helmholtz_eos(ctx, lastIndex - firstIndex, dim, Z.data(), detail::raw(d.temp, firstIndex),
+    detail::checkBurn(nnet_helmholtz_eos(ctx, lastIndex - firstIndex, dim, Z.data(), detail::raw(d.temp, firstIndex),
                                      detail::raw(d.rho, firstIndex), Y.data(), detail::raw(d.u, firstIndex),
                                      detail::raw(d.cv, firstIndex), detail::raw(d.p, firstIndex),
                                      detail::raw(d.c, firstIndex), detail::raw(d.dpdT, firstIndex), nullptr));

@@ -1,7 +1,7 @@
 """Build recipes for the oracle (test infrastructure only).
 
 * build_oracle(): compiles the CPU restatement oracle/nnet_oracle.cpp into
-  oracle/liboracle.so (g++ -O2 -fopenmp -ffp-contract=off).  Runs anywhere.
+  oracle/liboracle.so (g++ -O3 -fopenmp -ffp-contract=off).  Runs anywhere.
 * build_ref(): compiles the reference's own burn-path sources, as they lie under the
   reference tree, together with oracle/ref_driver.cpp into oracle/_ref/libnnet_ref.so.
   Only possible where the reference tree exists; the reference's CMake is bypassed
@@ -19,7 +19,9 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
 DATA = os.path.join(REPO, "sph-exa-nnet_gb300", "data")
-FLAGS = ["-O2", "-fopenmp", "-fPIC", "-shared", "-ffp-contract=off", "-w"]
+FLAGS = ["-O3", "-fopenmp", "-fPIC", "-shared", "-ffp-contract=off", "-w"]
+# the compiler line of the timed CPU baseline, as reported by bench.py
+CPU_FLAGS = "g++ " + " ".join(f for f in FLAGS if f not in ("-fPIC", "-shared", "-w"))
 
 
 def _newer(out, srcs):
@@ -41,7 +43,24 @@ def build_oracle(force=False):
     return out
 
 
-def build_ref(ref_root="/root/reference", force=False):
+def reference_root():
+    """The reference tree: $NNET_REFERENCE_ROOT, else the `reference_path` that the benchmark spec at
+    the repository root names, else None."""
+    root = os.environ.get("NNET_REFERENCE_ROOT")
+    if root:
+        return root
+    try:
+        import json
+        with open(os.path.join(REPO, "BASELINE.json")) as f:
+            return json.load(f).get("reference_path")
+    except (OSError, ValueError):
+        return None
+
+
+def build_ref(ref_root=None, force=False):
+    ref_root = ref_root or reference_root()
+    if not ref_root:
+        return None
     inc = os.path.join(ref_root, "include")
     if not os.path.isdir(inc):
         return None

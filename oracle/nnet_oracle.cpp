@@ -1040,7 +1040,7 @@ void prepareFromGuess(const Ctx& c, double* Mp, double* RHS, double* rates, cons
     Mp[0]  = 1 - kTheta * value_1 / e.cv;
 }
 
-// dense Gaussian elimination without pivoting (nnet_util/eigen.hpp:155-198)
+// dense Gaussian elimination without pivoting (nnet_util/eigen.hpp:178-223)
 void denseSolve(double* M, double* RHS, double* X, int n, double eps)
 {
     for (int i = 0; i < n; ++i)

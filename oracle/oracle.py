@@ -113,3 +113,35 @@ class Oracle:
         self._eosb(P, Y.shape[0], _ptr(Z), _ptr(T), _ptr(rho), _ptr(Y), _ptr(u), _ptr(cv), _ptr(p), _ptr(c),
                    _ptr(dpdT), nthreads)
         return dict(u=u, cv=cv, p=p, c=c, dpdT=dpdT)
+
+
+def compare_burns(net, Y0, g, o, tol=1e-8):
+    """Per-particle comparison of a GPU burn g = (Y, T, dt, status) with the oracle's o (same
+    layout) of the same inputs Y0: relative error of T, of every Y_i > 1e-12 and of the released
+    energy E = sum_i BE_i (Y_i - Y0_i) (test infrastructure: the checker of bench.py's baseline
+    leg).  Returns a dict of summary figures."""
+    import workloads
+    Yg, Tg, _, sg = g[:4]
+    Yo, To, _, so = o[:4]
+    BE = workloads.binding_energies(net)[: Yg.shape[0], None]
+    A = np.asarray(workloads.mass_numbers(net), dtype=np.float64)[: Yg.shape[0], None]
+    Eg, Eo = (BE * (Yg - Y0)).sum(0), (BE * (Yo - Y0)).sum(0)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        relT = np.abs(Tg - To) / np.abs(To)
+        big = Yo > 1e-12
+        relY = np.where(big, np.abs(Yg - Yo) / np.where(big, Yo, 1), 0).max(0)
+        relE = np.where(np.abs(Eo) > 0, np.abs(Eg - Eo) / np.abs(Eo), np.abs(Eg - Eo))
+    same = sg == so
+    tiny_E = np.abs(Eo) < 1e-30 * np.abs(BE).max()
+    ok = same & (relT <= tol) & (relY <= tol) & ((relE <= tol) | tiny_E)
+    flip = same & ~ok
+    dX = (np.abs(Yg - Yo) * A).max(0)
+    drift_g, drift_o = (A * Yg).sum(0) - 1, (A * Yo).sum(0) - 1
+    mx = lambda a, m: float(a[m].max()) if m.any() else 0.0
+    return {"particles": int(sg.size), "within_tol": float(ok.mean()), "tol": tol,
+            "status_agree": float(same.mean()), "max_rel_T_within": mx(relT, ok), "max_rel_Y_within": mx(relY, ok),
+            "max_rel_E_within": mx(relE, ok), "flipped": int(flip.sum()), "flipped_max_rel_T": mx(relT, flip),
+            "flipped_max_abs_dX": mx(dX, flip), "flipped_max_rel_Y": mx(relY, flip),
+            "sum_x_drift_max_gpu": float(np.abs(drift_g).max()) if sg.size else 0.0,
+            "sum_x_drift_max_oracle": float(np.abs(drift_o).max()) if sg.size else 0.0,
+            "sum_x_drift_max_diff": float(np.abs(drift_g - drift_o).max()) if sg.size else 0.0}

@@ -1,5 +1,5 @@
 // Test infrastructure, not product code: a C driver around the reference's own
-// burn-path sources, compiled (by oracle/build_ref.sh) together with
+// burn-path sources, compiled (by build_ref() in oracle/build.py) together with
 //   include/nnet/parameterization/net14/net14.cpp
 //   include/nnet/parameterization/net86/net86.cpp
 //   include/nnet/parameterization/net87/net87.cpp

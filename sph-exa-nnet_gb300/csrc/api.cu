@@ -10,7 +10,7 @@
 #include <string>
 #include <vector>
 
-#include "physics.cuh"
+#include "driver.cuh"
 #include "launch.hpp"
 #include "sparse_plan.hpp"
 #include "context.hpp"
@@ -84,7 +84,9 @@ int uploadNetwork(int net, NetBuffer& b)
         zf[4 * i + 0] = std::sqrt(z), zf[4 * i + 1] = std::sqrt(std::sqrt(z));
         zf[4 * i + 2] = std::pow(z, 1.9885), zf[4 * i + 3] = z > 0 ? std::log(z) : 0.;
     }
+    const double* Am  = net == 14 ? net14_A : net86_A; // net86_A[86] = 0 is the net87 electron entry
     const size_t oBE = putd(BE, N), oZ = putd(Z, net == 14 ? 14 : 87), oZ53 = putd(z53.data(), N);
+    const size_t oA  = putd(Am, net == 14 ? 14 : 87);
     const size_t oZf = putd(zf.data(), zf.size());
     const size_t oFit = putd(fit, nfit), oQ = putd(q, nq), oCh = putd(choose, nchoose);
     // partition-function ratio of every fitted rate per temperature range (the same IEEE
@@ -153,6 +155,7 @@ int uploadNetwork(int net, NetBuffer& b)
     v.net = net, v.nspec = N, v.nreact = R;
     v.rbeg = I + oRb, v.rspec = I + oRs, v.rcnt = I + oRc, v.pbeg = I + oPb, v.pspec = I + oPs, v.pcnt = I + oPc;
     v.BE = D + oBE, v.Z = D + oZ, v.z53 = D + oZ53, v.fit = D + oFit, v.q = D + oQ, v.choose = D + oCh;
+    v.A = D + oA;
     v.zFac = D + oZf, v.part = D + oPart;
     v.mainReactant = I + oMr, v.secondaryReactant = I + oSr, v.mainProduct = I + oMp;
     v.eLogT = D + oLT, v.eLogRho = D + oLR, v.eRate = D + oER;
@@ -184,6 +187,7 @@ int uploadNetwork(int net, NetBuffer& b)
 }
 
 constexpr int kNetCounters = 16;             // queue head + stats of one launch
+static_assert(1 + kStatWords <= kNetCounters, "counter region too small");
 constexpr int kCounters    = 4 * kNetCounters; // single launch uses [0, 16); a batch one region per network
 
 int netIndex(int net) { return net == 14 ? 0 : net == 86 ? 1 : net == 87 ? 2 : -1; }
@@ -198,6 +202,13 @@ struct EosParams
     const double *T, *rho;
     double *      u, *cv, *p, *c, *dpdT;
 };
+
+// post-burn steps of launches whose kernel does not fuse them (one thread per particle)
+__global__ void postBurnKernel(BurnParams bp, NetView nv, HelmView hv)
+{
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < bp.P; i += (size_t)gridDim.x * blockDim.x)
+        postScalar(bp, nv, hv, i, bp.status[i] != ST_SKIPPED);
+}
 
 __global__ void helmholtzEosKernel(EosParams ep, HelmView hv)
 {
@@ -236,7 +247,7 @@ int nnet_solver_info(int network, int solver, long long* factor_fma, long long* 
     const int n = network + 1;
     if (solver == NNET_SOLVER_DENSE_FP64)
     {
-        // eigen::solve with complete fill (eigen.hpp:155-198): elimination of row i by rows
+        // eigen::solve with complete fill (eigen.hpp:178-223): elimination of row i by rows
         // j < i costs 1 + (n - 1 - j) multiply-adds, back substitution n(n-1)/2
         long long f = 0;
         for (int i = 0; i < n; ++i)
@@ -298,6 +309,7 @@ int nnet_destroy(nnet_handle h)
     for (auto& n : h->nets)
         if (n.mem) cudaFree(n.mem);
     if (h->helmMem) cudaFree(h->helmMem);
+    if (h->orderCounters) cudaFree(h->orderCounters);
     h->ws.release();
     delete h;
     return NNET_SUCCESS;
@@ -349,11 +361,19 @@ int nnet_load_helmholtz_table(nnet_handle h, const double* table)
 int nnet_load_helmholtz_table_file(nnet_handle h, const char* path)
 {
     if (!h || !path) return fail(NNET_ERR_INVALID, "null argument");
-    std::ifstream f(path);
+    std::ifstream f(path, std::ios::binary);
     if (!f) return fail(NNET_ERR_FILE, std::string("cannot open ") + path);
     std::stringstream ss;
     ss << f.rdbuf();
     std::string s = ss.str();
+    constexpr size_t kBinaryBytes = (size_t)21 * HELM_IMAX * HELM_JMAX * sizeof(double);
+    if (s.size() == kBinaryBytes && s.find("STR(") == std::string::npos)
+    {
+        // the binary layout of nnet_load_helmholtz_table (little-endian doubles)
+        std::vector<double> tab(kBinaryBytes / sizeof(double));
+        std::memcpy(tab.data(), s.data(), kBinaryBytes);
+        return nnet_load_helmholtz_table(h, tab.data());
+    }
     // accept the STR( ... ) wrapper the reference #includes (helmholtz.cpp:92-94)
     size_t a = s.find("STR(");
     if (a != std::string::npos)
@@ -415,11 +435,36 @@ int nnet_gb300::Workspace::ensure(size_t need, cudaStream_t st)
     return NNET_SUCCESS;
 }
 
+int nnet_gb300::Workspace::ensureStatus(size_t P, cudaStream_t st)
+{
+    if (P > statusCap)
+    {
+        NNET_CUDA(cudaStreamSynchronize(st));
+        if (status) cudaFree(status);
+        status = nullptr, statusCap = 0;
+        NNET_CUDA(cudaMalloc(&status, P * sizeof(int32_t)));
+        statusCap = P;
+    }
+    return NNET_SUCCESS;
+}
+
 void nnet_gb300::Workspace::release()
 {
     if (scratch) cudaFree(scratch);
     if (counters) cudaFree(counters);
-    scratch = nullptr, counters = nullptr, doubles = 0;
+    if (status) cudaFree(status);
+    scratch = nullptr, counters = nullptr, doubles = 0, status = nullptr, statusCap = 0;
+}
+
+int nnet_gb300::launchPostBurn(const BurnParams& bp, const NetView& nv, const HelmView& hv, int numSMs,
+                               cudaStream_t st)
+{
+    if (!bp.postSteps() || bp.P == 0) return NNET_SUCCESS;
+    const int    block  = 128;
+    const size_t blocks = std::min<size_t>((bp.P + block - 1) / block, (size_t)numSMs * 16);
+    postBurnKernel<<<(unsigned)blocks, block, 0, st>>>(bp, nv, hv);
+    NNET_CUDA(cudaGetLastError());
+    return NNET_SUCCESS;
 }
 
 int nnet_gb300::occupancy(const KernelInfo& ki, int& perSM)
@@ -430,13 +475,13 @@ int nnet_gb300::occupancy(const KernelInfo& ki, int& perSM)
     return NNET_SUCCESS;
 }
 
-KernelInfo nnet_gb300::burnKernel(nnet_context* h, int net, int eos, int solver)
+KernelInfo nnet_gb300::burnKernel(nnet_context* h, int net, int eos, int solver, bool post)
 {
     if (solver == NNET_SOLVER_DENSE_FP64) return denseKernel(net, eos);
     const int mixed = solver == NNET_SOLVER_MIXED;
     if (h->layout == NNET_LAYOUT_THREAD) return sparseKernel(net, eos, mixed);
     if (h->layout == NNET_LAYOUT_WARP) return warpKernel(net, eos, mixed);
-    return batchKernel(net, eos, mixed);
+    return batchKernel(net, eos, mixed, post);
 }
 
 size_t nnet_gb300::maxScratchDoubles(nnet_context* h, int solver)
@@ -471,6 +516,13 @@ int validate(nnet_context* h, const nnet_burn_args* a)
         if (!a->Y[j]) return fail(NNET_ERR_INVALID, "null species pointer");
     if (!(a->hydro_dt > 0)) return fail(NNET_ERR_INVALID, "hydro_dt must be > 0");
     if (a->use_drhodt && !(a->previous_dt != 0)) return fail(NNET_ERR_INVALID, "use_drhodt needs previous_dt != 0");
+    const int eosOut = !!a->u + !!a->cv + !!a->p + !!a->c + !!a->dpdT;
+    if (eosOut != 0 && eosOut != 5) return fail(NNET_ERR_INVALID, "post-burn EOS needs all of u, cv, p, c, dpdT");
+    if (eosOut && !h->helmLoaded) return fail(NNET_ERR_NO_TABLE, "post-burn EOS requested before a Helmholtz table");
+    if (!(a->time_limit_seconds <= 0) && !(a->time_limit_seconds < 1e9))
+        return fail(NNET_ERR_INVALID, "time_limit_seconds must be finite");
+    if (a->num_particles > 0xffffffffull && a->order)
+        return fail(NNET_ERR_TOO_LARGE, "a visiting order holds 32-bit indices");
     return NNET_SUCCESS;
 }
 
@@ -485,7 +537,10 @@ void fillParams(const nnet_burn_args* a, unsigned long long* counters, BurnParam
     bp.useDrhodt = a->use_drhodt && a->rho_m1;
     bp.maxIter   = a->max_newton_iterations > 0 ? a->max_newton_iterations : 100000;
     bp.status = a->status, bp.substeps = a->substeps, bp.iterations = a->iterations;
-    bp.queue = counters, bp.stats = counters + 1, bp.order = nullptr;
+    bp.queue = counters, bp.stats = counters + 1, bp.order = a->order;
+    bp.timeLimitNs = a->time_limit_seconds > 0 ? std::max(1ull, (unsigned long long)(a->time_limit_seconds * 1e9)) : 0;
+    bp.normalize = a->normalize_mass != 0, bp.massDrift = a->mass_drift;
+    bp.eosU = a->u, bp.eosCv = a->cv, bp.eosP = a->p, bp.eosC = a->c, bp.eosDpdT = a->dpdT;
 }
 
 // persistent grid of `ki` for P particles: (blocks, slots)
@@ -510,7 +565,8 @@ int nnet_gb300::launchBurn(nnet_context* h, const nnet_burn_args* a, Workspace& 
     if (a->num_particles == 0) return NNET_SUCCESS;
     NNET_CUDA(cudaSetDevice(h->device));
     const int  ni = netIndex(a->network);
-    const KernelInfo ki = burnKernel(h, a->network, a->eos, a->solver);
+    const bool post = a->normalize_mass || a->mass_drift || a->u;
+    const KernelInfo ki = burnKernel(h, a->network, a->eos, a->solver, post);
     if (ki.maxNnz && h->nets[ni].plan.nnz > ki.maxNnz)
         return fail(NNET_ERR_TOO_LARGE, "sparse factor does not fit the kernel's storage");
     size_t blocks, slots;
@@ -522,6 +578,14 @@ int nnet_gb300::launchBurn(nnet_context* h, const nnet_burn_args* a, Workspace& 
     if (rs) bp.rs = *rs;
     bp.sliceIters = sliceIters, bp.segOf = nullptr, bp.segFinished = segFinished;
     bp.laneSlots  = h->laneSlots;
+    if (sliceIters > 0 && bp.postSteps())
+        return fail(NNET_ERR_INVALID, "post-burn steps are not available for sliced (served) launches");
+    const bool postPass = bp.postSteps() && !ki.fusedPost;
+    if (postPass && !bp.status)
+    {
+        if (int rc = ws.ensureStatus(a->num_particles, st)) return rc;
+        bp.status = ws.status;
+    }
 
     NNET_CUDA(cudaMemsetAsync(ws.counters, 0, kCounters * sizeof(unsigned long long), st));
     NetView  nv     = h->nets[ni].view;
@@ -530,6 +594,7 @@ int nnet_gb300::launchBurn(nnet_context* h, const nnet_burn_args* a, Workspace& 
     size_t   stride = slots;
     void*    args[] = {&bp, &nv, &hv, &sc, &stride};
     NNET_CUDA(cudaLaunchKernel(ki.func, dim3((unsigned)blocks), dim3(ki.block), args, ki.smem, st));
+    if (postPass) return launchPostBurn(bp, nv, hv, h->numSMs, st);
     return NNET_SUCCESS;
 }
 
@@ -576,24 +641,30 @@ extern "C" int nnet_burn_batch(nnet_handle h, const nnet_burn_args* batches, int
     }
     if (total == 0) return NNET_SUCCESS;
     NNET_CUDA(cudaSetDevice(h->device));
-    cudaStream_t st = (cudaStream_t)stream;
-    // thread layout: dense and sparse FP64 only (its mixed-precision multi-network form
-    // disagreed with the per-network burns on a few percent of c3 particles, cause not found)
-    const bool   tpp = batches[0].solver == NNET_SOLVER_DENSE_FP64 ||
-                     (h->layout == NNET_LAYOUT_THREAD && batches[0].solver == NNET_SOLVER_SPARSE_FP64);
-    KernelInfo   ki  = tpp ? multiKernel(batches[0].eos, batches[0].solver)
-                           : batchMultiKernel(batches[0].eos, batches[0].solver == NNET_SOLVER_MIXED);
+    cudaStream_t st   = (cudaStream_t)stream;
+    bool         post = false;
+    for (int k = 0; k < count; ++k)
+        post |= batches[k].num_particles > 0 && (batches[k].normalize_mass || batches[k].mass_drift || batches[k].u);
+    const bool tpp = batches[0].solver == NNET_SOLVER_DENSE_FP64 || h->layout == NNET_LAYOUT_THREAD;
+    KernelInfo ki  = tpp ? multiKernel(batches[0].eos, batches[0].solver)
+                         : batchMultiKernel(batches[0].eos, batches[0].solver == NNET_SOLVER_MIXED, post);
     for (int ni = 0; ni < 3; ++ni)
         if (mp.active[ni] && ki.maxNnz && h->nets[ni].plan.nnz > ki.maxNnz)
             return fail(NNET_ERR_TOO_LARGE, "sparse factor does not fit the kernel's storage");
     size_t blocks, slots;
     if (int rc = gridFor(h, ki, total, blocks, slots)) return rc;
     if (int rc = h->ws.ensure(slots * ki.perSlot, st)) return rc;
+    const bool postPass = post && !ki.fusedPost;
+    if (postPass)
+        if (int rc = h->ws.ensureStatus(total, st)) return rc;
+    size_t statusOff = 0;
     for (int k = 0; k < count; ++k)
     {
         const int ni = netIndex(batches[k].network);
         fillParams(batches + k, h->ws.counters + kNetCounters * (ni + 1), mp.bp[ni]);
         mp.bp[ni].laneSlots = h->laneSlots;
+        if (postPass && mp.bp[ni].postSteps() && !mp.bp[ni].status)
+            mp.bp[ni].status = h->ws.status + statusOff, statusOff += batches[k].num_particles;
     }
     NNET_CUDA(cudaMemsetAsync(h->ws.counters, 0, kCounters * sizeof(unsigned long long), st));
     HelmView hv     = h->helm;
@@ -603,6 +674,10 @@ extern "C" int nnet_burn_batch(nnet_handle h, const nnet_burn_args* batches, int
     NNET_CUDA(cudaLaunchKernel(ki.func, dim3((unsigned)blocks), dim3(ki.block), args, ki.smem, st));
     h->lastStream = st;
     h->lastMulti  = true;
+    if (postPass)
+        for (int ni = 0; ni < 3; ++ni)
+            if (mp.active[ni])
+                if (int rc = launchPostBurn(mp.bp[ni], mp.nv[ni], hv, h->numSMs, st)) return rc;
     return NNET_SUCCESS;
 }
 
@@ -618,12 +693,15 @@ int nnet_get_stats(nnet_handle h, nnet_stats* out)
     for (int r = h->lastMulti ? 1 : 0; r < (h->lastMulti ? 4 : 1); ++r)
         for (int k = 0; k < kNetCounters; ++k)
             v[k] += all[r * kNetCounters + k];
-    out->newton_iterations = v[1];
-    out->substeps          = v[2];
-    for (int s = 0; s < 5; ++s)
-        out->status_count[s] = v[3 + s];
-    out->refinement_steps = v[8];
-    out->fp64_fallbacks   = v[9];
+    const unsigned long long* w = v + 1; // [0] is the queue head
+    out->newton_iterations = w[kStatIters];
+    out->substeps          = w[kStatSubsteps];
+    for (int s = 0; s < kNumStatus; ++s)
+        out->status_count[s] = w[kStatStatus + s];
+    out->refinement_steps = w[kStatRefine];
+    out->fp64_fallbacks   = w[kStatFallback];
+    if (out->status_count[ST_ABORTED])
+        return fail(NNET_ERR_ABORTED, "the last launch stopped at its time limit (time_limit_seconds)");
     return NNET_SUCCESS;
 }
 

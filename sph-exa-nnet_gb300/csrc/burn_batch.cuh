@@ -1,4 +1,6 @@
-// Batched-warp forms of the sparse and mixed-precision burn: each warp carries 32
+// Batched-warp forms of the sparse and mixed-precision burn (templates; instantiated per
+// network in burn_batch14.cu, burn_batch86.cu, burn_batch87.cu and, for the multi-network
+// launch, burn_batch_multi_*.cu): each warp carries 32
 // particles in lockstep, one per lane, through Newton iterations.
 //
 // A Newton iteration has two kinds of work.  The per-particle scalar part (temperature
@@ -16,6 +18,8 @@
 //   S3 (lanes)     acceptance, rejection and timestep control; release / replace
 // Abundances and the slot table live in per-warp global scratch (L2-resident); one Newton
 // system per warp lives in shared memory.
+#pragma once
+
 #include "burn_multi.hpp"
 #include "launch.hpp"
 #include "warp_system.cuh"
@@ -52,11 +56,12 @@ __device__ __forceinline__ int specialSlot(int net, int k)
 
 enum : int
 {
-    ACT_ACCEPT = 1, // Y <- clipped candidate
-    ACT_CONT   = 2, // Yn <- clipped candidate
-    ACT_WRITE  = 4, // write the slot's Y back to the particle arrays (particle pw)
-    ACT_LOAD   = 8, // load a newly acquired particle's Y
-    ACT_BLEND  = 16 // θ-blend for the iteration about to run
+    ACT_ACCEPT = 1,  // Y <- clipped candidate
+    ACT_CONT   = 2,  // Yn <- clipped candidate
+    ACT_WRITE  = 4,  // write the slot's Y back to the particle arrays (particle pw)
+    ACT_LOAD   = 8,  // load a newly acquired particle's Y
+    ACT_BLEND  = 16, // θ-blend for the iteration about to run
+    ACT_FINAL  = 32  // the write ends particle pw's burn (not a pause): post-burn steps apply
 };
 
 template<int NET>
@@ -65,8 +70,11 @@ constexpr int padN()
     return (NET + 3) & ~3;
 }
 
-// take the next particle of the queue for this lane (skipped ones are completed here)
-__device__ bool acquireLane(const BurnParams& bp, ParticleState& s)
+// take the next particle of the queue for this lane; skipped ones, and once the launch is
+// past its time limit the remaining ones, are completed here by the lane alone
+template<bool POST>
+__device__ bool acquireLane(const BurnParams& bp, const NetView& nv, const HelmView& hv, ParticleState& s,
+                            unsigned long long deadline)
 {
     for (;;)
     {
@@ -76,13 +84,11 @@ __device__ bool acquireLane(const BurnParams& bp, ParticleState& s)
         const int    phase = bp.rs.phase ? bp.rs.phase[p] : 0;
         if (phase == 2) continue;
         const double rho = bp.rho[p], T = bp.T[p];
-        if (phase == 0 && !(rho > k::minRho && T > k::minTemp))
+        const bool   skip = phase == 0 && !(rho > k::minRho && T > k::minTemp);
+        if (skip || expired(deadline))
         {
-            if (bp.status) bp.status[p] = ST_SKIPPED;
-            if (bp.substeps) bp.substeps[p] = 0;
-            if (bp.iterations) bp.iterations[p] = 0;
-            atomicAdd(bp.stats + 2 + ST_SKIPPED, 1ull);
-            finishSegment(bp, p);
+            if constexpr (POST) postScalar(bp, nv, hv, p, !skip);
+            endUntouched(bp, p, skip ? ST_SKIPPED : ST_ABORTED);
             continue;
         }
         s.p = p, s.T = T, s.dt = bp.dt[p], s.rho = rho, s.i = 1;
@@ -111,7 +117,7 @@ __device__ void releaseLane(const BurnParams& bp, const ParticleState& s, int st
     const size_t p = s.p;
     bp.T[p]        = s.T;
     bp.dt[p]       = s.dt;
-    atomicAdd(bp.stats + 0, (unsigned long long)(s.nit - s.nit0));
+    atomicAdd(bp.stats + kStatIters, (unsigned long long)(s.nit - s.nit0));
     if (st == kPaused)
     {
         const ResumeState& r = bp.rs;
@@ -123,9 +129,39 @@ __device__ void releaseLane(const BurnParams& bp, const ParticleState& s, int st
     if (bp.status) bp.status[p] = st;
     if (bp.substeps) bp.substeps[p] = s.nsub;
     if (bp.iterations) bp.iterations[p] = (int32_t)s.nit;
-    atomicAdd(bp.stats + 1, (unsigned long long)s.nsub);
-    atomicAdd(bp.stats + 2 + st, 1ull);
+    atomicAdd(bp.stats + kStatSubsteps, (unsigned long long)s.nsub);
+    atomicAdd(bp.stats + kStatStatus + st, 1ull);
     finishSegment(bp, p);
+}
+
+// Post-burn steps of the slot's finished particle po, by the whole warp, on the abundances
+// yw[t] = Y[lane + 32 t] of its last accepted substep: s = sum_i A_i Y_i (fixed reduction
+// order), the drift s - 1, Y / s written back when normalising, and the sums the EOS needs
+// (returned to lane l).  Same steps as postScalar.
+template<int N>
+__device__ void postWarp(const BurnParams& bp, const NetView& nv, const double (&yw)[(N + 31) / 32], double sx,
+                         size_t po, int l, int lane, double& abW, double& zbW)
+{
+    sx = warpSum(sx);
+    if (lane == l && bp.massDrift) bp.massDrift[po] = sx - 1.;
+    const bool scale = bp.normalize && sx > 0 && sx < INFINITY;
+    double     ab = 0, zb = 0;
+#pragma unroll
+    for (int t = 0; t < (N + 31) / 32; ++t)
+    {
+        const int j = lane + 32 * t;
+        if (j < N)
+        {
+            const double y = scale ? yw[t] / sx : yw[t];
+            bp.Y[j][po]    = y;
+            ab += y, zb += y * __ldg(nv.Z + j);
+        }
+    }
+    if (bp.eosU)
+    {
+        ab = warpSum(ab), zb = warpSum(zb);
+        if (lane == l) abW = ab, zbW = zb;
+    }
 }
 
 // S2: everything of one Newton iteration that depends on (T, rho) of the slot only
@@ -311,7 +347,7 @@ constexpr int perWarpDoubles()
 // memory (perWarpDoubles<NET, MIXED>() or more); VS: abundance doubles per slot (at least
 // 2 * padN<NET>()).  Global warp gw owns scratch + gw * 32 * (VS + kSlotFields): its 32 slots'
 // abundances (slot l at l * VS: Y then Yn), then its slot table (32 * kSlotFields).
-template<int NET, int EOS, bool MIXED>
+template<int NET, int EOS, bool MIXED, bool POST>
 __device__ void batchLoop(const BurnParams& bp, const NetView& nv, const HelmView& hv, double* scratch, int VS,
                           double* wb)
 {
@@ -329,8 +365,9 @@ __device__ void batchLoop(const BurnParams& bp, const NetView& nv, const HelmVie
     const size_t  first  = (bp.P + warps - 1) / warps;
     // particles in flight per warp (fewer shorten each particle's iteration latency)
     const size_t  spw    = bp.laneSlots > 0 && bp.laneSlots < 32 ? (size_t)bp.laneSlots : 32;
+    const unsigned long long deadline = launchDeadline(bp);
     ParticleState s;
-    bool          has = (size_t)lane < (first < spw ? first : spw) && acquireLane(bp, s);
+    bool has = (size_t)lane < (first < spw ? first : spw) && acquireLane<POST>(bp, nv, hv, s, deadline);
     int           act = has ? ACT_LOAD : 0;
     size_t        pw  = 0;
     double        Tth = 0, rhoT = 0, used = 0, abar = 0, zbar = 0, yElec = 0, xT = 0;
@@ -348,6 +385,8 @@ __device__ void batchLoop(const BurnParams& bp, const NetView& nv, const HelmVie
                 st = ST_MAXITER;
             else if (bp.sliceIters > 0 && s.i == 1 && s.nit - s.nit0 >= bp.sliceIters)
                 st = kPaused;
+            else if (expired(deadline))
+                st = ST_ABORTED;
             else
             {
                 rhoT = s.rho - s.drho * (dtTot - s.elapsed);
@@ -365,31 +404,48 @@ __device__ void batchLoop(const BurnParams& bp, const NetView& nv, const HelmVie
             }
             releaseLane(bp, s, st);
             if (act & ACT_LOAD)
+            {
                 act &= ~ACT_LOAD; // never loaded: the particle arrays still hold its state
+                if constexpr (POST)
+                    if (st >= 0) postScalar(bp, nv, hv, s.p, true);
+            }
             else
-                act |= ACT_WRITE, pw = s.p;
-            has = acquireLane(bp, s);
+                act = (act & ~ACT_FINAL) | ACT_WRITE | (st >= 0 ? ACT_FINAL : 0), pw = s.p;
+            has = acquireLane<POST>(bp, nv, hv, s, deadline);
             if (has) act |= ACT_LOAD;
         }
 
         // ---- V1: per slot, pending updates, write-back / load, θ-blend
-        const int a0 = act | (cont ? ACT_BLEND : 0);
+        constexpr int JN  = (D::N + 31) / 32;
+        const int     a0  = act | (cont ? ACT_BLEND : 0);
+        double        abW = 0, zbW = 0; // post-burn EOS sums of this lane's finished particle
         for (unsigned m = __ballot_sync(kFull, a0 != 0); m; m &= m - 1)
         {
-            const int    l  = __ffs(m) - 1;
-            const int    a  = __shfl_sync(kFull, a0, l);
-            const size_t po = __shfl_sync(kFull, (unsigned long long)pw, l);
-            const size_t pn = __shfl_sync(kFull, (unsigned long long)s.p, l);
-            const int    il = __shfl_sync(kFull, s.i, l);
-            double*      v  = vec0 + l * VS;
-            double*      vn = v + NP;
-            double       ab = 0, zb = 0, ynLast = 0;
-            for (int j = lane; j < D::N; j += 32)
+            const int    l    = __ffs(m) - 1;
+            const int    a    = __shfl_sync(kFull, a0, l);
+            const size_t po   = __shfl_sync(kFull, (unsigned long long)pw, l);
+            const size_t pn   = __shfl_sync(kFull, (unsigned long long)s.p, l);
+            const int    il   = __shfl_sync(kFull, s.i, l);
+            double*      v    = vec0 + l * VS;
+            double*      vn   = v + NP;
+            const bool   post = POST && (a & ACT_FINAL);
+            double       ab = 0, zb = 0, ynLast = 0, sx = 0;
+            double       yw[JN];
+#pragma unroll
+            for (int t = 0; t < JN; ++t)
             {
+                const int j = lane + 32 * t;
+                if (j >= D::N) break;
                 double y = v[j], yn = vn[j];
                 if (a & ACT_ACCEPT) y = yn <= k::epsilonVector ? 0. : yn;
                 if (a & ACT_CONT) yn = yn <= k::epsilonVector ? 0. : yn;
-                if (a & ACT_WRITE) bp.Y[j][po] = y;
+                if (a & ACT_WRITE)
+                {
+                    if (post)
+                        yw[t] = y, sx += y * __ldg(nv.A + j);
+                    else
+                        bp.Y[j][po] = y;
+                }
                 if (a & ACT_LOAD) y = bp.Y[j][pn];
                 if (a & ACT_BLEND)
                 {
@@ -398,6 +454,8 @@ __device__ void batchLoop(const BurnParams& bp, const NetView& nv, const HelmVie
                 }
                 v[j] = y, vn[j] = yn, ynLast = yn;
             }
+            if constexpr (POST)
+                if (post) postWarp<D::N>(bp, nv, yw, sx, po, l, lane, abW, zbW);
             if (a & ACT_BLEND)
             {
                 ab = warpSum(ab), zb = warpSum(zb);
@@ -406,6 +464,9 @@ __device__ void batchLoop(const BurnParams& bp, const NetView& nv, const HelmVie
                 if (lane == l) abar = ab, zbar = zb, yElec = NET == 87 ? ye : 0.;
             }
         }
+        // post-burn EOS of the particles finished by this lane (lane-parallel)
+        if constexpr (POST)
+            if (bp.eosU && (a0 & ACT_FINAL)) postEos(bp, hv, pw, abW, zbW);
         act = 0;
 
         // ---- S2: EOS and the (T, rho)-only rate factors of every running slot
@@ -431,10 +492,10 @@ __device__ void batchLoop(const BurnParams& bp, const NetView& nv, const HelmVie
                 if (steps < 0)
                 {
                     warpSolve64<NET, MIXED>(nv, S, lane); // not settled: this system is solved in FP64
-                    if (lane == 0) atomicAdd(bp.stats + 8, 1ull);
+                    if (lane == 0) atomicAdd(bp.stats + kStatFallback, 1ull);
                 }
                 else if (steps && lane == 0)
-                    atomicAdd(bp.stats + 7, (unsigned long long)steps);
+                    atomicAdd(bp.stats + kStatRefine, (unsigned long long)steps);
             }
             else
                 warpSolve64<NET, MIXED>(nv, S, lane);
@@ -522,8 +583,8 @@ __device__ void batchLoop(const BurnParams& bp, const NetView& nv, const HelmVie
             if (st >= 0)
             {
                 releaseLane(bp, s, st);
-                act |= ACT_WRITE, pw = s.p;
-                has = acquireLane(bp, s);
+                act |= ACT_WRITE | ACT_FINAL, pw = s.p;
+                has = acquireLane<POST>(bp, nv, hv, s, deadline);
                 if (has) act |= ACT_LOAD;
             }
         }
@@ -531,68 +592,72 @@ __device__ void batchLoop(const BurnParams& bp, const NetView& nv, const HelmVie
     }
 }
 
-template<int NET, int EOS, bool MIXED>
+template<int NET, int EOS, bool MIXED, bool POST>
 __global__ void __launch_bounds__(32, 9) burnBatchKernel(BurnParams bp, NetView nv, HelmView hv, double* scratch,
                                                       size_t /*unused*/)
 {
     extern __shared__ __align__(16) double smem[];
     double* wb = smem + (size_t)(threadIdx.x >> 5) * perWarpDoubles<NET, MIXED>();
-    batchLoop<NET, EOS, MIXED>(bp, nv, hv, scratch, 2 * padN<NET>(), wb);
+    batchLoop<NET, EOS, MIXED, POST>(bp, nv, hv, scratch, 2 * padN<NET>(), wb);
 }
 
 // One launch over sub-batches of different networks (the uneven mixed workload): every warp
 // drains the net86 queue, then net87, then net14, so the expensive particles start first and
 // the cheap ones fill the tail.  A warp changes network once all its lanes are idle.
-template<int EOS, bool MIXED>
+template<int EOS, bool MIXED, bool POST>
 __global__ void __launch_bounds__(32, 9) burnBatchMultiKernel(MultiParams mp, HelmView hv, double* scratch,
                                                            size_t /*unused*/)
 {
     extern __shared__ __align__(16) double smem[];
     double*       wb = smem + (size_t)(threadIdx.x >> 5) * perWarpDoubles<87, MIXED>();
     constexpr int VS = 2 * padN<87>();
-    if (mp.active[1]) batchLoop<86, EOS, MIXED>(mp.bp[1], mp.nv[1], hv, scratch, VS, wb);
-    if (mp.active[2]) batchLoop<87, EOS, MIXED>(mp.bp[2], mp.nv[2], hv, scratch, VS, wb);
-    if (mp.active[0]) batchLoop<14, EOS, MIXED>(mp.bp[0], mp.nv[0], hv, scratch, VS, wb);
+    if (mp.active[1]) batchLoop<86, EOS, MIXED, POST>(mp.bp[1], mp.nv[1], hv, scratch, VS, wb);
+    if (mp.active[2]) batchLoop<87, EOS, MIXED, POST>(mp.bp[2], mp.nv[2], hv, scratch, VS, wb);
+    if (mp.active[0]) batchLoop<14, EOS, MIXED, POST>(mp.bp[0], mp.nv[0], hv, scratch, VS, wb);
 }
 
-namespace
-{
-template<int NET, int EOS, bool MIXED>
+// Registry entries: slot scratch per thread, shared memory per one-warp block.  `post`
+// selects the instantiation that applies the post-burn steps as particles retire.
+template<int NET, int EOS, bool MIXED, bool POST>
 KernelInfo batchInfo()
 {
     // lanesPerParticle = 32: a small batch is spread one particle per warp over the grid
-    return {(const void*)burnBatchKernel<NET, EOS, MIXED>, (size_t)2 * padN<NET>() + kSlotFields, 32,
-            WDims<NET>::NNZ, perWarpDoubles<NET, MIXED>() * sizeof(double), 32};
+    return {(const void*)burnBatchKernel<NET, EOS, MIXED, POST>, (size_t)2 * padN<NET>() + kSlotFields, 32,
+            WDims<NET>::NNZ, perWarpDoubles<NET, MIXED>() * sizeof(double), 32, true};
 }
 
-template<int EOS, bool MIXED>
+template<int NET>
+KernelInfo pickBatchNet(int eos, int mixed, bool post)
+{
+    if (eos)
+    {
+        if (mixed) return post ? batchInfo<NET, 1, true, true>() : batchInfo<NET, 1, true, false>();
+        return post ? batchInfo<NET, 1, false, true>() : batchInfo<NET, 1, false, false>();
+    }
+    if (mixed) return post ? batchInfo<NET, 0, true, true>() : batchInfo<NET, 0, true, false>();
+    return post ? batchInfo<NET, 0, false, true>() : batchInfo<NET, 0, false, false>();
+}
+
+template<int EOS, bool MIXED, bool POST>
 KernelInfo batchMultiInfo()
 {
     static_assert(perWarpDoubles<87, MIXED>() >= perWarpDoubles<86, MIXED>() &&
                       perWarpDoubles<87, MIXED>() >= perWarpDoubles<14, MIXED>(),
                   "net87 has the largest warp layout");
-    return {(const void*)burnBatchMultiKernel<EOS, MIXED>, (size_t)2 * padN<87>() + kSlotFields, 32,
-            WDims<87>::NNZ, perWarpDoubles<87, MIXED>() * sizeof(double), 32};
+    return {(const void*)burnBatchMultiKernel<EOS, MIXED, POST>, (size_t)2 * padN<87>() + kSlotFields, 32,
+            WDims<87>::NNZ, perWarpDoubles<87, MIXED>() * sizeof(double), 32, true};
 }
 
-template<bool MIXED>
-KernelInfo pickBatch(int net, int eos)
+template<int EOS>
+KernelInfo pickBatchMulti(int mixed, bool post)
 {
-    if (net == 14) return eos ? batchInfo<14, 1, MIXED>() : batchInfo<14, 0, MIXED>();
-    if (net == 86) return eos ? batchInfo<86, 1, MIXED>() : batchInfo<86, 0, MIXED>();
-    return eos ? batchInfo<87, 1, MIXED>() : batchInfo<87, 0, MIXED>();
-}
-} // namespace
-
-KernelInfo batchKernel(int net, int eos, int mixed)
-{
-    return mixed ? pickBatch<true>(net, eos) : pickBatch<false>(net, eos);
+    if (mixed) return post ? batchMultiInfo<EOS, true, true>() : batchMultiInfo<EOS, true, false>();
+    return post ? batchMultiInfo<EOS, false, true>() : batchMultiInfo<EOS, false, false>();
 }
 
-KernelInfo batchMultiKernel(int eos, int mixed)
-{
-    if (mixed) return eos ? batchMultiInfo<1, true>() : batchMultiInfo<0, true>();
-    return eos ? batchMultiInfo<1, false>() : batchMultiInfo<0, false>();
-}
+// per-slot doubles of the batched layout's scratch (the largest network's)
+constexpr size_t kBatchSlotDoubles = (size_t)2 * padN<87>() + kSlotFields;
+static_assert(kBatchSlotDoubles <= kNoallocSlotDoubles, "nnet_burn_noalloc's fixed slots are too small");
 
 } // namespace nnet_gb300
+

@@ -14,26 +14,50 @@
 namespace nnet_gb300
 {
 
+// Element index of the FP32 region shared by the three networks' slots (mixed form): above
+// the FP64 rows of the largest network, so that no slot's FP32 rows overlap the FP64 rows of
+// a slot running another network (see SparsePolicy's constructor).
+template<int FORM>
+constexpr size_t multiFloatBase()
+{
+    if constexpr (FORM == NNET_SOLVER_DENSE_FP64)
+        return 0;
+    else
+        return std::max({SparsePolicy<14, true>::doubleElems(), SparsePolicy<86, true>::doubleElems(),
+                         SparsePolicy<87, true>::doubleElems()});
+}
+
+template<int NET, int FORM>
+__device__ __forceinline__ typename PolicyOf<NET, FORM>::type multiPolicy(const BurnParams& bp, double* scratch,
+                                                                       size_t stride, size_t slot)
+{
+    if constexpr (FORM == NNET_SOLVER_DENSE_FP64)
+        return typename PolicyOf<NET, FORM>::type(scratch, stride, slot);
+    else
+    {
+        typename PolicyOf<NET, FORM>::type pol(scratch, stride, slot, multiFloatBase<FORM>());
+        if constexpr (FORM == NNET_SOLVER_MIXED) pol.refineStats = bp.stats + kStatRefine;
+        return pol;
+    }
+}
+
 template<int EOS, int FORM>
 __global__ void __launch_bounds__(128) burnMultiKernel(MultiParams mp, HelmView hv, double* scratch, size_t stride)
 {
     const size_t slot = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (mp.active[1])
     {
-        typename PolicyOf<86, FORM>::type pol(scratch, stride, slot);
-        if constexpr (FORM == NNET_SOLVER_MIXED) pol.refineStats = mp.bp[1].stats + 7;
+        auto pol = multiPolicy<86, FORM>(mp.bp[1], scratch, stride, slot);
         burnLoop<86, EOS>(mp.bp[1], mp.nv[1], hv, pol);
     }
     if (mp.active[2])
     {
-        typename PolicyOf<87, FORM>::type pol(scratch, stride, slot);
-        if constexpr (FORM == NNET_SOLVER_MIXED) pol.refineStats = mp.bp[2].stats + 7;
+        auto pol = multiPolicy<87, FORM>(mp.bp[2], scratch, stride, slot);
         burnLoop<87, EOS>(mp.bp[2], mp.nv[2], hv, pol);
     }
     if (mp.active[0])
     {
-        typename PolicyOf<14, FORM>::type pol(scratch, stride, slot);
-        if constexpr (FORM == NNET_SOLVER_MIXED) pol.refineStats = mp.bp[0].stats + 7;
+        auto pol = multiPolicy<14, FORM>(mp.bp[0], scratch, stride, slot);
         burnLoop<14, EOS>(mp.bp[0], mp.nv[0], hv, pol);
     }
 }
@@ -41,8 +65,11 @@ __global__ void __launch_bounds__(128) burnMultiKernel(MultiParams mp, HelmView 
 template<int EOS, int FORM>
 static KernelInfo multiInfo()
 {
-    const size_t s = std::max({PolicyOf<14, FORM>::type::perSlot(), PolicyOf<86, FORM>::type::perSlot(),
-                               PolicyOf<87, FORM>::type::perSlot()});
+    size_t s = std::max({PolicyOf<14, FORM>::type::perSlot(), PolicyOf<86, FORM>::type::perSlot(),
+                         PolicyOf<87, FORM>::type::perSlot()});
+    if constexpr (FORM == NNET_SOLVER_MIXED)
+        s = multiFloatBase<FORM>() + std::max({SparsePolicy<14, true>::floatElems(), SparsePolicy<86, true>::floatElems(),
+                                               SparsePolicy<87, true>::floatElems()});
     return {(const void*)burnMultiKernel<EOS, FORM>, s, 128, PolicyOf<86, FORM>::maxNnz};
 }
 

@@ -4,7 +4,7 @@
 //
 // Plain FP64 form of the burn: the Newton system is assembled densely and solved by
 // Gaussian elimination without pivoting, in the reference's operation order
-// (include/nnet/nuclear_net.hpp:347-438 and :514-609, include/nnet_util/eigen.hpp:155-198).
+// (include/nnet/nuclear_net.hpp:347-438 and :514-609, include/nnet_util/eigen.hpp:178-223).
 // One thread per particle; the (N+1)^2 matrix and the vectors live in per-slot scratch,
 // interleaved across slots so that every access of a warp is one coalesced 256-byte line.
 //
@@ -171,7 +171,7 @@ struct DensePolicy
         RHS[0] = T * value1 / cv;
         M[0]   = 1 - k::theta * value1 / cv;
 
-        // Gaussian elimination without pivoting, zero multipliers skipped (eigen.hpp:155-198)
+        // Gaussian elimination without pivoting, zero multipliers skipped (eigen.hpp:178-223)
         for (int i = 0; i < n; ++i)
         {
             for (int j = 0; j < i; ++j)
@@ -228,12 +228,17 @@ struct SparsePolicy
     Strided<double> A, b, x, r, Y, Yn, rates, drates, BE, dYdt, dYdT, jdy, ipiv, scale;
     Strided<float>  LU, d32;
 
-    static constexpr size_t perSlot()
-    {
-        return (size_t)MAXNNZ + 5 * D::n + 2 * D::N + 2 * D::R + 4 * D::N + (MIXED ? (MAXNNZ + D::n + 1) / 2 + 1 : 0);
-    }
+    // per-slot doubles: the FP64 vectors, then (mixed form) the FP32 factor and correction
+    static constexpr size_t doubleElems() { return (size_t)MAXNNZ + 5 * D::n + 2 * D::N + 2 * D::R + 4 * D::N; }
+    static constexpr size_t floatElems() { return MIXED ? (MAXNNZ + D::n + 1) / 2 + 1 : 0; }
+    static constexpr size_t perSlot() { return doubleElems() + floatElems(); }
 
-    __device__ SparsePolicy(double* scratch, size_t stride, size_t slot)
+    // floatBase: element index (in doubles) where the FP32 region of every slot starts.  The
+    // FP32 rows interleave across slots at half the FP64 row width, so row e of slot s lands in
+    // the FP64 row floatBase + (e * stride + s) / (2 * stride): another slot's column.  Every
+    // slot of a launch must therefore use the same floatBase, at or above the FP64 rows of every
+    // network that any slot of the launch runs (a multi-network launch passes the maximum).
+    __device__ SparsePolicy(double* scratch, size_t stride, size_t slot, size_t floatBase = doubleElems())
     {
         A      = {scratch + slot, stride};
         b      = A.at(MAXNNZ);
@@ -249,9 +254,9 @@ struct SparsePolicy
         dYdt   = BE.at(D::N);
         dYdT   = dYdt.at(D::N);
         jdy    = dYdT.at(D::N);
-        double* f = jdy.at(D::N).p; // float region: 2 floats per double row
-        LU     = {reinterpret_cast<float*>(f - slot) + slot, stride};
-        // floats interleave with the same slot stride; element e of slot s at f0[e*stride + s]
+        // float region: element e of slot s at f0[e * stride + s], f0 = the float view of
+        // FP64 row floatBase (2 floats per double row)
+        LU  = {reinterpret_cast<float*>(scratch + floatBase * stride) + slot, stride};
         d32 = LU.at(MAXNNZ);
     }
 

@@ -12,7 +12,7 @@ __global__ void __launch_bounds__(128) burnSparseKernel(BurnParams bp, NetView n
 {
     const size_t              slot = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     SparsePolicy<NET, MIXED> pol(scratch, stride, slot);
-    pol.refineStats = bp.stats + 7;
+    pol.refineStats = bp.stats + kStatRefine;
     burnLoop<NET, EOS>(bp, nv, hv, pol);
 }
 

@@ -162,7 +162,8 @@ __global__ void __launch_bounds__(128) burnWarpKernel(BurnParams bp, NetView nv,
     WarpSmem<NET, MIXED> S(base);
     const SparseView& sp = nv.sp;
 
-    ParticleState s;
+    const unsigned long long deadline = launchDeadline(bp);
+    ParticleState            s;
     for (;;)
     {
         // ---- acquire (lane 0 takes the queue index; every lane then reads the same words)
@@ -174,16 +175,11 @@ __global__ void __launch_bounds__(128) burnWarpKernel(BurnParams bp, NetView nv,
         const int    phase = bp.rs.phase ? bp.rs.phase[p] : 0;
         if (phase == 2) continue;
         const double rho0 = bp.rho[p], T0 = bp.T[p];
-        if (phase == 0 && !(rho0 > k::minRho && T0 > k::minTemp))
+        const bool skip = phase == 0 && !(rho0 > k::minRho && T0 > k::minTemp);
+        const bool late = __shfl_sync(kFull, (int)expired(deadline), 0) != 0;
+        if (skip || late)
         {
-            if (lane == 0)
-            {
-                if (bp.status) bp.status[p] = ST_SKIPPED;
-                if (bp.substeps) bp.substeps[p] = 0;
-                if (bp.iterations) bp.iterations[p] = 0;
-                atomicAdd(bp.stats + 2 + ST_SKIPPED, 1ull);
-                finishSegment(bp, p);
-            }
+            if (lane == 0) endUntouched(bp, p, skip ? ST_SKIPPED : ST_ABORTED);
             continue;
         }
         for (int j = lane; j < D::N; j += 32)
@@ -218,6 +214,11 @@ __global__ void __launch_bounds__(128) burnWarpKernel(BurnParams bp, NetView nv,
             if (bp.sliceIters > 0 && s.i == 1 && s.nit - s.nit0 >= bp.sliceIters)
             {
                 st = kPaused;
+                break;
+            }
+            if (deadline && __shfl_sync(kFull, (int)expired(deadline), 0))
+            {
+                st = ST_ABORTED;
                 break;
             }
             const double dtTot = bp.hydroDt;
@@ -256,10 +257,10 @@ __global__ void __launch_bounds__(128) burnWarpKernel(BurnParams bp, NetView nv,
                 {
                     // not settled: re-solve this system in FP64 (A and b are intact)
                     warpSolve64<NET, MIXED>(nv, S, lane);
-                    if (lane == 0) atomicAdd(bp.stats + 8, 1ull);
+                    if (lane == 0) atomicAdd(bp.stats + kStatFallback, 1ull);
                 }
                 else if (steps && lane == 0)
-                    atomicAdd(bp.stats + 7, (unsigned long long)steps);
+                    atomicAdd(bp.stats + kStatRefine, (unsigned long long)steps);
             }
             else
                 warpSolve64<NET, MIXED>(nv, S, lane);
@@ -359,7 +360,7 @@ __global__ void __launch_bounds__(128) burnWarpKernel(BurnParams bp, NetView nv,
         {
             bp.T[p]  = s.T;
             bp.dt[p] = s.dt;
-            atomicAdd(bp.stats + 0, (unsigned long long)(s.nit - s.nit0));
+            atomicAdd(bp.stats + kStatIters, (unsigned long long)(s.nit - s.nit0));
             if (st == kPaused)
             {
                 const ResumeState& r = bp.rs;
@@ -372,8 +373,8 @@ __global__ void __launch_bounds__(128) burnWarpKernel(BurnParams bp, NetView nv,
                 if (bp.status) bp.status[p] = st;
                 if (bp.substeps) bp.substeps[p] = s.nsub;
                 if (bp.iterations) bp.iterations[p] = (int32_t)s.nit;
-                atomicAdd(bp.stats + 1, (unsigned long long)s.nsub);
-                atomicAdd(bp.stats + 2 + st, 1ull);
+                atomicAdd(bp.stats + kStatSubsteps, (unsigned long long)s.nsub);
+                atomicAdd(bp.stats + kStatStatus + st, 1ull);
                 finishSegment(bp, p);
             }
         }

@@ -77,6 +77,7 @@ struct NetView
     int           net, nspec, nreact;
     const int *   rbeg, *rspec, *rcnt, *pbeg, *pspec, *pcnt;
     const double *BE, *Z, *z53;
+    const double* A; // mass numbers (net87: the electron entry is 0)
     // per species i: sqrt(z53), sqrt(sqrt(z53)), z53^1.9885, log(z53) (fast rate forms)
     const double* zFac;
     const double *fit, *q, *choose;
@@ -105,7 +106,28 @@ enum : int32_t
     ST_LIVELOCK = NNET_PARTICLE_LIVELOCK,
     ST_MAXITER  = NNET_PARTICLE_MAXITER,
     ST_ZERO_DT  = NNET_PARTICLE_ZERO_DT,
+    ST_ABORTED  = NNET_PARTICLE_ABORTED,
+    kNumStatus  = NNET_NUM_PARTICLE_STATUS,
 };
+
+// Word offsets of a launch's statistics (BurnParams::stats)
+enum : int
+{
+    kStatIters    = 0,                        // Newton iterations
+    kStatSubsteps = 1,                        // accepted substeps
+    kStatStatus   = 2,                        // [kStatStatus + s]: particles ending with status s
+    kStatRefine   = kStatStatus + kNumStatus, // mixed form: refinement steps
+    kStatFallback = kStatRefine + 1,          // mixed form: systems re-solved in FP64
+    kStatWords    = kStatFallback + 1
+};
+
+// %globaltimer (ns) of the calling thread's SM
+__device__ __forceinline__ unsigned long long globalTimerNs()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 
 // Per-particle state that lets a burn pause at an attempt boundary and resume later with
 // bit-identical arithmetic (continuous batching).  phase: 0 not started, 1 paused,
@@ -135,9 +157,17 @@ struct BurnParams
     int32_t*       substeps;
     int32_t*       iterations;
     unsigned long long* queue;  // work-queue head (reset to 0 before each launch)
-    unsigned long long* stats;  // [0] Newton iterations, [1] substeps, [2+s] status counts,
-                                // [7] refinement steps, [8] FP64 fallbacks
+    unsigned long long* stats;  // kStatWords counters (kStatIters ... kStatFallback)
     const uint32_t*     order;  // optional particle visiting order (nullptr: identity)
+    // launch watchdog: 0, or the nanoseconds after which the launch takes no further Newton
+    // iteration (running particles stop at their last accepted substep, queued ones untouched,
+    // both with ST_ABORTED)
+    unsigned long long  timeLimitNs;
+    // post-burn steps (all optional): divide Y by sum_i A_i Y_i, report sum_i A_i Y_i - 1 of
+    // the burned state, Helmholtz EOS at the final state (computeHelmEOS)
+    int                 normalize;
+    double*             massDrift;
+    double *            eosU, *eosCv, *eosP, *eosC, *eosDpdT;
     // continuous batching (all optional): resumable state, Newton-iteration budget of this
     // launch per particle (a particle pauses at the first attempt boundary past it), and a
     // per-particle segment id whose finished-particle counter is incremented on completion
@@ -146,6 +176,8 @@ struct BurnParams
     const int*          segOf;
     unsigned long long* segFinished;
     int                 laneSlots; // batched layout: particles in flight per warp (0 = 32)
+
+    __host__ __device__ bool postSteps() const { return normalize || massDrift || eosU; }
 };
 
 } // namespace nnet_gb300

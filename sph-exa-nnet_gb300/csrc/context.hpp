@@ -2,6 +2,7 @@
 // the C ABI and the burn server.
 #pragma once
 
+#include <algorithm>
 #include <cuda_runtime.h>
 
 #include "common.cuh"
@@ -26,9 +27,16 @@ struct Workspace
     double*             scratch  = nullptr;
     size_t              doubles  = 0;
     unsigned long long* counters = nullptr; // [0] queue head, [1..] stats (BurnParams::stats)
+    int32_t*            status    = nullptr; // per-particle statuses when the caller passes none
+    size_t              statusCap = 0;       //   and a post-burn pass needs them
     int                 ensure(size_t need, cudaStream_t st);
+    int                 ensureStatus(size_t P, cudaStream_t st);
     void                release();
 };
+
+// Post-burn steps (BurnParams::postSteps) of a launch whose kernel does not fuse them: one
+// thread per particle after the burn, on `st`; bp.status must hold every particle's status.
+int launchPostBurn(const BurnParams& bp, const NetView& nv, const HelmView& hv, int numSMs, cudaStream_t st);
 
 // Launch one burn over args->num_particles particles on `st` with workspace `ws`.
 // rs / sliceIters / segFinished enable pausing and resuming (see BurnParams).
@@ -44,7 +52,7 @@ int  setError(int code, const char* msg);
 int occupancy(const KernelInfo& ki, int& perSM);
 
 // kernel of (network, eos, solver) under the context's layout
-KernelInfo burnKernel(struct ::nnet_context* h, int net, int eos, int solver);
+KernelInfo burnKernel(struct ::nnet_context* h, int net, int eos, int solver, bool post = false);
 
 // scratch doubles of the largest persistent grid of any network for `solver`
 size_t maxScratchDoubles(struct ::nnet_context* h, int solver);
@@ -63,4 +71,9 @@ struct nnet_context
     bool                   lastMulti  = false; // last launch was nnet_burn_batch
     int                    layout     = NNET_LAYOUT_AUTO;
     int                    laneSlots  = 32; // batched layout: particles in flight per warp
+    // device addresses of nnet_burn_noalloc's fixed arrays, looked up by its first call on this
+    // handle (they live as long as the device context the handle was created in)
+    double*                noallocScratch  = nullptr;
+    unsigned long long*    noallocCounters = nullptr;
+    unsigned long long*    orderCounters   = nullptr; // nnet_cost_order's bucket counters and cursors
 };

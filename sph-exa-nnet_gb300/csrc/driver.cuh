@@ -79,6 +79,53 @@ __device__ __forceinline__ void networkRates(const NetView& nv, Strided<double> 
         net87Rates(nv, Yg[86], T, rho, BE, rates, drates);
 }
 
+// Helmholtz EOS of the post-burn step, written to particle p's outputs (out of line: it runs
+// once per particle, and inlining it would add its registers to the burn loop's)
+static __device__ __noinline__ void postEos(const BurnParams& bp, const HelmView& hv, size_t p, double abar,
+                                            double zbar)
+{
+    const EosResult e = helmholtzEos(hv, abar, zbar, bp.T[p], bp.rho[p]);
+    bp.eosU[p] = e.u, bp.eosCv[p] = e.cv, bp.eosP[p] = e.p, bp.eosC[p] = e.c, bp.eosDpdT[p] = e.dpdT;
+}
+
+// Post-burn steps of particle p by one thread, on the state in the particle arrays:
+// s = sum_i A_i Y_i, reported as s - 1; Y_i <- Y_i / s when `normalize` (and s is positive
+// and finite); then the Helmholtz EOS at the final state over the network's charges
+// (computeHelmEOS, parallel_nuclear_net.hpp:191-261 with cudaKernelComputeHelmholtz,
+// CUDA/parallel_nuclear_net.cu:184-210).
+static __device__ __noinline__ void postScalar(const BurnParams& bp, const NetView& nv, const HelmView& hv, size_t p,
+                                               bool normalize)
+{
+    const int N  = nv.nspec;
+    double    sx = 0;
+    for (int j = 0; j < N; ++j)
+        sx += bp.Y[j][p] * __ldg(nv.A + j);
+    if (bp.massDrift) bp.massDrift[p] = sx - 1.;
+    const bool scale = normalize && bp.normalize && sx > 0 && sx < INFINITY;
+    double     ab = 0, zb = 0;
+    for (int j = 0; j < N; ++j)
+    {
+        double y = bp.Y[j][p];
+        if (scale)
+        {
+            y          = y / sx;
+            bp.Y[j][p] = y;
+        }
+        ab += y, zb += y * __ldg(nv.Z + j);
+    }
+    if (bp.eosU) postEos(bp, hv, p, ab, zb);
+}
+
+// launch watchdog: true once the launch has run past its time limit (deadline 0: no limit)
+__device__ __forceinline__ bool expired(unsigned long long deadline)
+{
+    return deadline != 0 && globalTimerNs() > deadline;
+}
+__device__ __forceinline__ unsigned long long launchDeadline(const BurnParams& bp)
+{
+    return bp.timeLimitNs ? globalTimerNs() + bp.timeLimitNs : 0;
+}
+
 // Fetch the next burnable particle; skipped ones (rho <= 1e5 or T <= 1e8,
 // parallel_nuclear_net_impl.cpp:83) are written back immediately.
 __device__ __forceinline__ void finishSegment(const BurnParams& bp, size_t p)
@@ -87,8 +134,19 @@ __device__ __forceinline__ void finishSegment(const BurnParams& bp, size_t p)
     if (bp.segFinished) atomicAdd(bp.segFinished + (bp.segOf ? bp.segOf[p] : 0), 1ull);
 }
 
+// A particle that ends without a Newton iteration: skipped (cold) or, once the launch is past
+// its time limit, aborted before it started; its state stays as it is.
+__device__ __forceinline__ void endUntouched(const BurnParams& bp, size_t p, int st)
+{
+    if (bp.status) bp.status[p] = st;
+    if (bp.substeps) bp.substeps[p] = 0;
+    if (bp.iterations) bp.iterations[p] = 0;
+    atomicAdd(bp.stats + kStatStatus + st, 1ull);
+    finishSegment(bp, p);
+}
+
 template<int NET, class Policy>
-__device__ bool acquire(const BurnParams& bp, Policy& pol, ParticleState& s)
+__device__ bool acquire(const BurnParams& bp, Policy& pol, ParticleState& s, unsigned long long deadline)
 {
     for (;;)
     {
@@ -100,11 +158,12 @@ __device__ bool acquire(const BurnParams& bp, Policy& pol, ParticleState& s)
         const double rho = bp.rho[p], T = bp.T[p];
         if (phase == 0 && !(rho > k::minRho && T > k::minTemp))
         {
-            if (bp.status) bp.status[p] = ST_SKIPPED;
-            if (bp.substeps) bp.substeps[p] = 0;
-            if (bp.iterations) bp.iterations[p] = 0;
-            atomicAdd(bp.stats + 2 + ST_SKIPPED, 1ull);
-            finishSegment(bp, p);
+            endUntouched(bp, p, ST_SKIPPED);
+            continue;
+        }
+        if (expired(deadline))
+        {
+            endUntouched(bp, p, ST_ABORTED);
             continue;
         }
         for (int j = 0; j < NET; ++j)
@@ -145,9 +204,9 @@ __device__ void release(const BurnParams& bp, Policy& pol, const ParticleState& 
     if (bp.status) bp.status[s.p] = status;
     if (bp.substeps) bp.substeps[s.p] = s.nsub;
     if (bp.iterations) bp.iterations[s.p] = (int32_t)s.nit;
-    atomicAdd(bp.stats + 0, (unsigned long long)(s.nit - s.nit0));
-    atomicAdd(bp.stats + 1, (unsigned long long)s.nsub);
-    atomicAdd(bp.stats + 2 + status, 1ull);
+    atomicAdd(bp.stats + kStatIters, (unsigned long long)(s.nit - s.nit0));
+    atomicAdd(bp.stats + kStatSubsteps, (unsigned long long)s.nsub);
+    atomicAdd(bp.stats + kStatStatus + status, 1ull);
     finishSegment(bp, s.p);
 }
 
@@ -161,7 +220,7 @@ __device__ void pause(const BurnParams& bp, Policy& pol, const ParticleState& s)
     r.elapsed[p] = s.elapsed, r.nextT[p] = s.nextT, r.drho[p] = s.drho, r.nit[p] = s.nit, r.nsub[p] = s.nsub;
     r.cdDt[p] = s.cdDt, r.cdNt[p] = s.cdNt, r.cdPower[p] = s.cdPower, r.cdSteps[p] = s.cdSteps;
     r.phase[p] = 1;
-    atomicAdd(bp.stats + 0, (unsigned long long)(s.nit - s.nit0));
+    atomicAdd(bp.stats + kStatIters, (unsigned long long)(s.nit - s.nit0));
 }
 
 constexpr int kPaused = -2;
@@ -170,9 +229,10 @@ constexpr int kPaused = -2;
 // final status.
 template<int NET, int EOS, class Policy>
 __device__ int newtonIteration(const BurnParams& bp, const NetView& nv, const HelmView& hv, Policy& pol,
-                               ParticleState& s)
+                               ParticleState& s, unsigned long long deadline)
 {
     if (s.nit >= bp.maxIter) return ST_MAXITER;
+    if (expired(deadline)) return ST_ABORTED;
     if (bp.sliceIters > 0 && s.i == 1 && s.nit - s.nit0 >= bp.sliceIters) return kPaused;
 
     // prepareSystemSubstep (nuclear_net.hpp:858-879)
@@ -280,20 +340,21 @@ __device__ int newtonIteration(const BurnParams& bp, const NetView& nv, const He
 template<int NET, int EOS, class Policy>
 __device__ __forceinline__ void burnLoop(const BurnParams& bp, const NetView& nv, const HelmView& hv, Policy& pol)
 {
-    ParticleState s;
-    bool          have = acquire<NET>(bp, pol, s);
+    const unsigned long long deadline = launchDeadline(bp);
+    ParticleState            s;
+    bool                     have = acquire<NET>(bp, pol, s, deadline);
     while (have)
     {
-        const int st = newtonIteration<NET, EOS>(bp, nv, hv, pol, s);
+        const int st = newtonIteration<NET, EOS>(bp, nv, hv, pol, s, deadline);
         if (st >= 0)
         {
             release<NET>(bp, pol, s, st);
-            have = acquire<NET>(bp, pol, s);
+            have = acquire<NET>(bp, pol, s, deadline);
         }
         else if (st == kPaused)
         {
             pause<NET>(bp, pol, s);
-            have = acquire<NET>(bp, pol, s);
+            have = acquire<NET>(bp, pol, s, deadline);
         }
     }
 }

@@ -15,13 +15,14 @@
 //   * scratch does not grow with the number of particles: the persistent grid is capped to the
 //     array's slots and the work queue feeds any number of particles through them; a launch whose
 //     slots would not fit the array is rejected with NNET_ERR_TOO_LARGE;
-//   * the first call on a device looks up the arrays' device addresses there (with that device
-//     current); make that first call before any stream capture;
+//   * the first call on a handle looks up the arrays' device addresses with the handle's device
+//     current and keeps them in the handle; make that first call before any stream capture;
 //   * every call shares the arrays: the counters are cleared on the caller's stream at the start
 //     of each call (the scratch needs no clearing: each slot loads its particle before use), and
-//     two calls that overlap on the GPU race on both; nnet_get_stats does not report these calls.
+//     two calls that overlap on the GPU race on both; nnet_get_stats does not report these calls;
+//   * the post-burn steps (normalize_mass, mass_drift, the EOS outputs) are applied by the
+//     kernel itself, so they need no extra memory either.
 #include <algorithm>
-#include <mutex>
 #include <string>
 
 #include "context.hpp"
@@ -31,51 +32,32 @@ namespace
 {
 using namespace nnet_gb300;
 
-constexpr size_t kSlots        = 4096; // particle slots in flight at most
-constexpr size_t kSlotDoubles  = 230;  // largest per-slot need of the batched kernels (net86, net87)
+constexpr size_t kSlots        = 4096;                // particle slots in flight at most
+constexpr size_t kSlotDoubles  = kNoallocSlotDoubles; // largest per-slot need of the batched kernels
 constexpr size_t kScratch      = kSlots * kSlotDoubles;
 constexpr int    kCounterWords = 16; // queue head + statistics (BurnParams::stats)
+static_assert(1 + kStatWords <= kCounterWords, "counter array too small");
 
 static __device__ __align__(256) double g_scratch[kScratch];
 static __device__ __align__(256) unsigned long long g_counters[kCounterWords];
-
-// device addresses of the arrays, per device
-struct DeviceArrays
-{
-    double*             scratch  = nullptr;
-    unsigned long long* counters = nullptr;
-};
-constexpr int kMaxDevices = 64;
-std::mutex    g_mutex;
-DeviceArrays  g_arrays[kMaxDevices];
-
-int deviceArrays(int device, DeviceArrays& out)
-{
-    if (device < 0 || device >= kMaxDevices) return setError(NNET_ERR_INVALID, "device index out of range");
-    std::lock_guard<std::mutex> lock(g_mutex);
-    DeviceArrays&               d = g_arrays[device];
-    if (!d.scratch)
-    {
-        // the current device is `device` (set by the caller)
-        void*       s = nullptr;
-        void*       c = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&s, g_scratch);
-        if (e == cudaSuccess) e = cudaGetSymbolAddress(&c, g_counters);
-        if (e != cudaSuccess)
-        {
-            std::string m = std::string("cudaGetSymbolAddress of the no-alloc arrays: ") + cudaGetErrorString(e);
-            return setError(NNET_ERR_CUDA, m.c_str());
-        }
-        d.scratch = static_cast<double*>(s), d.counters = static_cast<unsigned long long*>(c);
-    }
-    out = d;
-    return NNET_SUCCESS;
-}
 
 int cudaFail(cudaError_t e, const char* what)
 {
     std::string m = std::string(what) + ": " + cudaGetErrorString(e);
     return setError(NNET_ERR_CUDA, m.c_str());
+}
+
+// device addresses of the arrays in the handle's context (the handle's device is current)
+int deviceArrays(nnet_context* h)
+{
+    if (h->noallocScratch) return NNET_SUCCESS;
+    void* s = nullptr;
+    void* c = nullptr;
+    if (cudaError_t e = cudaGetSymbolAddress(&s, g_scratch)) return cudaFail(e, "cudaGetSymbolAddress(scratch)");
+    if (cudaError_t e = cudaGetSymbolAddress(&c, g_counters)) return cudaFail(e, "cudaGetSymbolAddress(counters)");
+    h->noallocScratch  = static_cast<double*>(s);
+    h->noallocCounters = static_cast<unsigned long long*>(c);
+    return NNET_SUCCESS;
 }
 } // namespace
 
@@ -86,11 +68,11 @@ extern "C" int nnet_burn_noalloc(nnet_handle h, const nnet_burn_args* a, void* s
         return setError(NNET_ERR_INVALID, "nnet_burn_noalloc runs the sparse and mixed solvers only");
     if (a->num_particles == 0) return NNET_SUCCESS;
     if (cudaError_t e = cudaSetDevice(h->device)) return cudaFail(e, "cudaSetDevice");
-    DeviceArrays d;
-    if (int rc = deviceArrays(h->device, d)) return rc;
+    if (int rc = deviceArrays(h)) return rc;
 
-    const KernelInfo ki = batchKernel(a->network, a->eos, a->solver == NNET_SOLVER_MIXED);
-    const int        ni = a->network == 14 ? 0 : a->network == 86 ? 1 : 2;
+    const bool       post = a->normalize_mass || a->mass_drift || a->u;
+    const KernelInfo ki   = batchKernel(a->network, a->eos, a->solver == NNET_SOLVER_MIXED, post);
+    const int        ni   = a->network == 14 ? 0 : a->network == 86 ? 1 : 2;
     if (ki.maxNnz && h->nets[ni].plan.nnz > ki.maxNnz)
         return setError(NNET_ERR_TOO_LARGE, "sparse factor does not fit the kernel's storage");
     int perSM = 0;
@@ -106,13 +88,14 @@ extern "C" int nnet_burn_noalloc(nnet_handle h, const nnet_burn_args* a, void* s
                                             "fixed scratch array (7.2 MiB)");
 
     BurnParams bp;
-    fillBurnParams(a, d.counters, bp);
+    fillBurnParams(a, h->noallocCounters, bp);
     bp.laneSlots = h->laneSlots;
     cudaStream_t st = (cudaStream_t)stream;
-    if (cudaError_t e = cudaMemsetAsync(d.counters, 0, sizeof(g_counters), st)) return cudaFail(e, "cudaMemsetAsync");
+    if (cudaError_t e = cudaMemsetAsync(h->noallocCounters, 0, sizeof(g_counters), st))
+        return cudaFail(e, "cudaMemsetAsync");
     NetView  nv     = h->nets[ni].view;
     HelmView hv     = h->helm;
-    double*  sc     = d.scratch;
+    double*  sc     = h->noallocScratch;
     size_t   stride = slots;
     void*    args[] = {&bp, &nv, &hv, &sc, &stride};
     if (cudaError_t e = cudaLaunchKernel(ki.func, dim3((unsigned)blocks), dim3(ki.block), args, ki.smem, st))

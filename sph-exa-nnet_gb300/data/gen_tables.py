@@ -5,7 +5,10 @@ present on the development machine) and writes its output beside this script.  T
 generated header is committed; the build never needs the reference at run time.
 
 usage: python gen_tables.py [REFERENCE_ROOT]
+(default: $NNET_REFERENCE_ROOT, else the reference_path that the benchmark spec at the repository
+root names)
 """
+import json
 import os
 import subprocess
 import sys
@@ -14,7 +17,16 @@ import tempfile
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
-def main(ref_root="/root/reference"):
+def reference_root():
+    root = os.environ.get("NNET_REFERENCE_ROOT")
+    if root:
+        return root
+    with open(os.path.join(HERE, "..", "..", "BASELINE.json")) as f:
+        return json.load(f)["reference_path"]
+
+
+def main(ref_root=None):
+    ref_root = ref_root or reference_root()
     inc = os.path.join(ref_root, "include")
     par = os.path.join(inc, "nnet", "parameterization")
     electron = os.path.join(par, "net87", "electron_rate.dat")

@@ -30,7 +30,8 @@ EOS_IDEAL_GAS, EOS_HELMHOLTZ = 0, 1
 SOLVER_DENSE_FP64, SOLVER_SPARSE_FP64, SOLVER_MIXED = 0, 1, 2
 LAYOUT_AUTO, LAYOUT_THREAD, LAYOUT_WARP, LAYOUT_BATCHED = 0, 1, 2, 3
 LAYOUTS = {"auto": LAYOUT_AUTO, "thread": LAYOUT_THREAD, "warp": LAYOUT_WARP, "batched": LAYOUT_BATCHED}
-STATUS_NAMES = ["OK", "SKIPPED", "LIVELOCK", "MAXITER", "ZERO_DT"]
+STATUS_NAMES = ["OK", "SKIPPED", "LIVELOCK", "MAXITER", "ZERO_DT", "ABORTED"]
+ERR_ABORTED = -6
 NUM_REACTIONS = {14: 29, 86: 309, 87: 311}
 SOLVERS = {"dense": SOLVER_DENSE_FP64, "plain": SOLVER_DENSE_FP64, "sparse": SOLVER_SPARSE_FP64,
            "mixed": SOLVER_MIXED}
@@ -47,13 +48,57 @@ class _BurnArgs(ctypes.Structure):
                 ("rho_m1", ctypes.c_void_p), ("dt", ctypes.c_void_p), ("hydro_dt", ctypes.c_double),
                 ("previous_dt", ctypes.c_double), ("use_drhodt", ctypes.c_int),
                 ("max_newton_iterations", ctypes.c_longlong), ("status", ctypes.c_void_p),
-                ("substeps", ctypes.c_void_p), ("iterations", ctypes.c_void_p)]
+                ("substeps", ctypes.c_void_p), ("iterations", ctypes.c_void_p),
+                ("time_limit_seconds", ctypes.c_double), ("normalize_mass", ctypes.c_int),
+                ("mass_drift", ctypes.c_void_p), ("u", ctypes.c_void_p), ("cv", ctypes.c_void_p),
+                ("p", ctypes.c_void_p), ("c", ctypes.c_void_p), ("dpdT", ctypes.c_void_p),
+                ("order", ctypes.c_void_p)]
 
 
 class _Stats(ctypes.Structure):
     _fields_ = [("newton_iterations", ctypes.c_ulonglong), ("substeps", ctypes.c_ulonglong),
-                ("status_count", ctypes.c_ulonglong * 5), ("refinement_steps", ctypes.c_ulonglong),
+                ("status_count", ctypes.c_ulonglong * len(STATUS_NAMES)), ("refinement_steps", ctypes.c_ulonglong),
                 ("fp64_fallbacks", ctypes.c_ulonglong)]
+
+
+def _dptr(t):
+    return None if t is None else t.data_ptr()
+
+
+def burn_args(network, Y, T, rho, dt, hydro_dt, eos=EOS_HELMHOLTZ, mu=0.0, rho_m1=None, previous_dt=0.0,
+              use_drhodt=False, solver=SOLVER_DENSE_FP64, max_iter=100000, status=None, substeps=None,
+              iterations=None, time_limit=0.0, normalize_mass=False, mass_drift=None, eos_out=None, order=None):
+    """The nnet_burn_args of a burn (CUDA tensors; Y a list of per-species tensors or a 2-D
+    [species, particles] tensor).  Returns (args, keep): `keep` holds the pointer array the
+    arguments refer to and must outlive the call.  eos_out: None or the five tensors
+    (u, cv, p, c, dpdT) of the post-burn Helmholtz EOS; order: None or an int32 CUDA tensor
+    holding a permutation of the particle indices (the work queue's visiting order)."""
+    import torch
+    if isinstance(solver, str):
+        solver = SOLVERS[solver]
+    if isinstance(eos, str):
+        eos = EOS_IDEAL_GAS if eos.startswith("ideal") else EOS_HELMHOLTZ
+    rows = [Y[j] for j in range(network)]
+    outs = list(eos_out) if eos_out is not None else [None] * 5
+    if len(outs) != 5:
+        raise NnetError("eos_out needs the five tensors u, cv, p, c, dpdT")
+    named = [("T", T), ("rho", rho), ("dt", dt), ("rho_m1", rho_m1), ("mass_drift", mass_drift)]
+    named += [("Y", r) for r in rows] + list(zip(["u", "cv", "p", "c", "dpdT"], outs))
+    for name, t in named:
+        _require_cuda(t, name)
+        if t is not None and t.dtype != torch.float64:
+            raise NnetError(f"{name} must be float64")
+    if order is not None and (order.dtype != torch.int32 or order.numel() != T.numel() or not order.is_cuda):
+        raise NnetError("order must be an int32 CUDA tensor of num_particles indices")
+    yp = (ctypes.c_void_p * network)(*[r.data_ptr() for r in rows])
+    a = _BurnArgs(network=network, eos=eos, ideal_gas_mu=mu, solver=solver, num_particles=T.numel(),
+                  Y=ctypes.cast(yp, ctypes.POINTER(ctypes.c_void_p)), T=T.data_ptr(), rho=rho.data_ptr(),
+                  rho_m1=_dptr(rho_m1), dt=dt.data_ptr(), hydro_dt=hydro_dt, previous_dt=previous_dt,
+                  use_drhodt=int(bool(use_drhodt)), max_newton_iterations=max_iter, status=_dptr(status),
+                  substeps=_dptr(substeps), iterations=_dptr(iterations), time_limit_seconds=time_limit,
+                  normalize_mass=int(bool(normalize_mass)), mass_drift=_dptr(mass_drift), u=_dptr(outs[0]),
+                  cv=_dptr(outs[1]), p=_dptr(outs[2]), c=_dptr(outs[3]), dpdT=_dptr(outs[4]), order=_dptr(order))
+    return a, yp
 
 
 _lib = None
@@ -82,6 +127,9 @@ def load_library(path=LIB_PATH):
     lib.nnet_measure_fp64_peak.argtypes = [I, ctypes.POINTER(D)]
     lib.nnet_set_layout.argtypes = [P, I]
     lib.nnet_set_batch_slots.argtypes = [P, I]
+    lib.nnet_burn_batch.argtypes = [P, ctypes.POINTER(_BurnArgs), I, P]
+    lib.nnet_burn_noalloc.argtypes = [P, ctypes.POINTER(_BurnArgs), P]
+    lib.nnet_cost_order.argtypes = [P, S, P, P, P]
     _lib = lib
     return lib
 
@@ -151,64 +199,67 @@ class Context:
 
     def burn(self, network, Y, T, rho, dt, hydro_dt, eos=EOS_HELMHOLTZ, mu=0.0, rho_m1=None, previous_dt=0.0,
              use_drhodt=False, solver=SOLVER_DENSE_FP64, max_iter=100000, status=None, substeps=None,
-             iterations=None, stream=None):
-        """Burn in place.  Y: list of per-species 1-D CUDA float64 tensors (or a 2-D
-        [species, particles] tensor); T, dt updated in place."""
+             iterations=None, stream=None, time_limit=0.0, normalize_mass=False, mass_drift=None, eos_out=None,
+             order=None):
+        """Burn in place (nnet_burn).  Y: list of per-species 1-D CUDA float64 tensors (or a 2-D
+        [species, particles] tensor); T, dt updated in place.  time_limit: launch watchdog in
+        seconds (0: none); normalize_mass / mass_drift / eos_out: the post-burn steps; order: the
+        work queue's visiting order."""
         import torch
-        if isinstance(solver, str):
-            solver = SOLVERS[solver]
-        if isinstance(eos, str):
-            eos = EOS_IDEAL_GAS if eos.startswith("ideal") else EOS_HELMHOLTZ
-        rows = [Y[j] for j in range(network)]
-        for name, t in [("T", T), ("rho", rho), ("dt", dt), ("rho_m1", rho_m1)] + [("Y", r) for r in rows]:
-            _require_cuda(t, name)
-            if t is not None and t.dtype != torch.float64:
-                raise NnetError(f"{name} must be float64")
-        P = T.numel()
-        yp = (ctypes.c_void_p * network)(*[r.data_ptr() for r in rows])
-        a = _BurnArgs(network=network, eos=eos, ideal_gas_mu=mu, solver=solver, num_particles=P,
-                      Y=ctypes.cast(yp, ctypes.POINTER(ctypes.c_void_p)), T=T.data_ptr(), rho=rho.data_ptr(),
-                      rho_m1=None if rho_m1 is None else rho_m1.data_ptr(), dt=dt.data_ptr(),
-                      hydro_dt=hydro_dt, previous_dt=previous_dt, use_drhodt=int(bool(use_drhodt)),
-                      max_newton_iterations=max_iter,
-                      status=None if status is None else status.data_ptr(),
-                      substeps=None if substeps is None else substeps.data_ptr(),
-                      iterations=None if iterations is None else iterations.data_ptr())
+        a, keep = burn_args(network, Y, T, rho, dt, hydro_dt, eos, mu, rho_m1, previous_dt, use_drhodt, solver,
+                            max_iter, status, substeps, iterations, time_limit, normalize_mass, mass_drift, eos_out,
+                            order)
         s = torch.cuda.current_stream(self.device) if stream is None else stream
         _check(_lib.nnet_burn(self.handle, ctypes.byref(a), ctypes.c_void_p(s.cuda_stream)))
 
-    def burn_batch(self, batches, solver=SOLVER_SPARSE_FP64, eos=EOS_HELMHOLTZ, mu=0.0, max_iter=100000, stream=None):
-        """One launch over sub-batches of different networks.  `batches`: list of dicts with
-        keys network, Y, T, rho, dt, hydro_dt and optional status / iterations (CUDA tensors)."""
+    def burn_batch(self, batches, solver=SOLVER_SPARSE_FP64, eos=EOS_HELMHOLTZ, mu=0.0, max_iter=100000, stream=None,
+                   normalize_mass=False):
+        """One launch over sub-batches of different networks (nnet_burn_batch).  `batches`: list of
+        dicts with keys network, Y, T, rho, dt, hydro_dt and optional status / iterations /
+        substeps / mass_drift / eos_out (CUDA tensors)."""
         import torch
-        if isinstance(solver, str):
-            solver = SOLVERS[solver]
-        if isinstance(eos, str):
-            eos = EOS_IDEAL_GAS if eos.startswith("ideal") else EOS_HELMHOLTZ
         arr = (_BurnArgs * len(batches))()
         keep = []
         for k, b in enumerate(batches):
-            net = b["network"]
-            yp = (ctypes.c_void_p * net)(*[b["Y"][j].data_ptr() for j in range(net)])
+            a, yp = burn_args(b["network"], b["Y"], b["T"], b["rho"], b["dt"], b["hydro_dt"], eos, mu, solver=solver,
+                              max_iter=max_iter, status=b.get("status"), substeps=b.get("substeps"),
+                              iterations=b.get("iterations"), normalize_mass=normalize_mass,
+                              mass_drift=b.get("mass_drift"), eos_out=b.get("eos_out"))
+            arr[k] = a
             keep.append(yp)
-            st, it = b.get("status"), b.get("iterations")
-            arr[k] = _BurnArgs(network=net, eos=eos, ideal_gas_mu=mu, solver=solver, num_particles=b["T"].numel(),
-                               Y=ctypes.cast(yp, ctypes.POINTER(ctypes.c_void_p)), T=b["T"].data_ptr(),
-                               rho=b["rho"].data_ptr(), rho_m1=None, dt=b["dt"].data_ptr(), hydro_dt=b["hydro_dt"],
-                               previous_dt=0.0, use_drhodt=0, max_newton_iterations=max_iter,
-                               status=None if st is None else st.data_ptr(), substeps=None,
-                               iterations=None if it is None else it.data_ptr())
         s = torch.cuda.current_stream(self.device) if stream is None else stream
-        lib = load_library()
-        lib.nnet_burn_batch.argtypes = [ctypes.c_void_p, ctypes.POINTER(_BurnArgs), ctypes.c_int, ctypes.c_void_p]
-        _check(lib.nnet_burn_batch(self.handle, arr, len(batches), ctypes.c_void_p(s.cuda_stream)))
+        _check(_lib.nnet_burn_batch(self.handle, arr, len(batches), ctypes.c_void_p(s.cuda_stream)))
+
+    def burn_noalloc(self, network, Y, T, rho, dt, hydro_dt, stream=None, **kw):
+        """nnet_burn_noalloc: the batched-layout burn with the library's fixed scratch arrays
+        (no device allocation); same keywords as burn (sparse and mixed solvers only)."""
+        import torch
+        a, keep = burn_args(network, Y, T, rho, dt, hydro_dt, **kw)
+        s = torch.cuda.current_stream(self.device) if stream is None else stream
+        _check(_lib.nnet_burn_noalloc(self.handle, ctypes.byref(a), ctypes.c_void_p(s.cuda_stream)))
+
+    def cost_order(self, cost, stream=None):
+        """nnet_cost_order: an int32 CUDA tensor holding a permutation of the particles with the
+        costliest first (decreasing power-of-two class of `cost`, an int32 CUDA tensor such as a
+        previous burn's iterations), for burn(order=...)."""
+        import torch
+        if cost.dtype != torch.int32 or not cost.is_cuda:
+            raise NnetError("cost must be an int32 CUDA tensor")
+        order = torch.empty_like(cost)
+        s = torch.cuda.current_stream(self.device) if stream is None else stream
+        _check(_lib.nnet_cost_order(self.handle, cost.numel(), _ptr(cost), _ptr(order), ctypes.c_void_p(s.cuda_stream)))
+        return order
 
     def stats(self):
+        """Statistics of the last burn on this context; `aborted` is True when that launch
+        stopped at its time limit (nnet_get_stats returned NNET_ERR_ABORTED)."""
         st = _Stats()
-        _check(_lib.nnet_get_stats(self.handle, ctypes.byref(st)))
+        rc = _lib.nnet_get_stats(self.handle, ctypes.byref(st))
+        if rc not in (0, ERR_ABORTED):
+            _check(rc)
         return dict(newton_iterations=st.newton_iterations, substeps=st.substeps,
                     status=dict(zip(STATUS_NAMES, list(st.status_count))), refinement_steps=st.refinement_steps,
-                    fp64_fallbacks=st.fp64_fallbacks)
+                    fp64_fallbacks=st.fp64_fallbacks, aborted=rc == ERR_ABORTED)
 
     def helmholtz_eos(self, Z, T, rho, Y, u, cv, p, c, dpdT, stream=None):
         import torch

@@ -9,9 +9,11 @@ the Newton-iteration count of its previous burn (returned per particle by the li
 (cost ~ 1 + log2(hydro_dt / dt)).  `partition` cuts the arrays into contiguous ranges of
 (nearly) equal predicted cost.
 
-Measured with the oracle on 4,096 c2 particles ordered by temperature (clustered), second
-burn, ratio of the slowest rank's Newton iterations to the mean, 2 / 4 / 8 ranks:
-equal-count ranges 1.20 / 2.16 / 3.82; previous-iteration cost 1.12 / 1.14 / 1.84."""
+This is host logic: bench.py --strong uses it to split one particle set over torchrun ranks,
+and tests/test_sharding.py checks (with the oracle, 2,048 c2 particles ordered by temperature,
+two consecutive burns) that ranges balanced on the first burn's iterations balance the second
+burn better than equal-count ranges; tests/test_multirank.py runs the split over two gloo
+ranks."""
 import numpy as np
 
 

@@ -38,6 +38,21 @@ def mass_numbers(net):
     return _A86[:86] if net == 86 else _A86
 
 
+_BE = {}
+
+
+def binding_energies(net):
+    """Binding energies of a network's species (the reference's BE tables)."""
+    if net not in _BE:
+        import os
+        import re
+        src = open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "nnet_network_tables.h")).read()
+        name = {14: "net14_BE", 86: "net86_BE", 87: "net87_BE"}[net]
+        body = re.search(name + r"\[\d+\] = \{([^}]*)\}", src).group(1)
+        _BE[net] = np.array([float(v) for v in body.split(",")])
+    return _BE[net]
+
+
 def composition(net, P, xc, xo, floor):
     """Y[species, P] from mass fractions X(12C)=xc, X(16O)=xo and a floor on the others."""
     A = mass_numbers(net)

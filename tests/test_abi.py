@@ -49,3 +49,25 @@ def test_library_is_sm103a_only():
     """The shared library carries sm_103a SASS (one -gencode)."""
     import nnet_build
     assert nnet_build.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def test_ctypes_structs_match_the_header(tmp_path):
+    """The Python mirror's nnet_burn_args / nnet_stats have the C header's field offsets and sizes."""
+    import subprocess
+    import nnet_gb300 as nn
+    structs = {"nnet_burn_args": nn._BurnArgs, "nnet_stats": nn._Stats}
+    lines = []
+    for cname, py in structs.items():
+        lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')
+        for f, _ in py._fields_:
+            lines.append(f'printf("{cname}.{f} %zu\\n", offsetof({cname}, {f}));')
+    src = tmp_path / "layout.c"
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "nnet_gb300.h"\nint main(void){\n'
+                   + "\n".join(lines) + "\nreturn 0;}\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", os.path.join(REPO, "include"), str(src), "-o", str(exe)], check=True)
+    c = dict(l.split() for l in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.splitlines())
+    for cname, py in structs.items():
+        assert int(c[cname]) == ctypes.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert int(c[f"{cname}.{f}"]) == getattr(py, f).offset, (cname, f)

@@ -68,3 +68,28 @@ def test_burn_in_cuda_graph(ctx):
         got = (Y.cpu().numpy(), T.cpu().numpy(), dt.cpu().numpy(), st.cpu().numpy())
         for a, b in zip(ref, got):
             assert np.array_equal(a, b)
+
+
+def test_cost_order_is_a_costliest_first_permutation_and_keeps_results(ctx):
+    """nnet_cost_order gives a permutation in decreasing power-of-two cost classes; a burn in
+    that visiting order gives the same per-particle results bit for bit."""
+    import torch
+    from test_gpu_parity import gpu_burn
+    dev = torch.device("cuda:0")
+    rng = np.random.default_rng(3)
+    cost = torch.tensor(rng.integers(0, 5000, 100003), dtype=torch.int32, device=dev)
+    order = ctx.cost_order(cost).cpu().numpy()
+    c = cost.cpu().numpy()
+    assert np.array_equal(np.sort(order), np.arange(c.size))
+    cls = np.floor(np.log2(np.maximum(c[order], 1)))
+    assert np.all(np.diff(cls) <= 0)
+    w = workloads.make("c2", P=2000, seed=31)
+    a = gpu_burn(ctx, w, "sparse")
+    o = ctx.cost_order(torch.tensor(a[5], device=dev))
+    Y, T = torch.tensor(w["Y"], device=dev), torch.tensor(w["T"], device=dev)
+    rho, dt = torch.tensor(w["rho"], device=dev), torch.tensor(w["dt"], device=dev)
+    st = torch.zeros(2000, dtype=torch.int32, device=dev)
+    ctx.burn(86, Y, T, rho, dt, w["hydro_dt"], solver="sparse", status=st, max_iter=20000, order=o)
+    torch.cuda.synchronize()
+    assert np.array_equal(Y.cpu().numpy(), a[0]) and np.array_equal(T.cpu().numpy(), a[1])
+    assert np.array_equal(st.cpu().numpy(), a[3])

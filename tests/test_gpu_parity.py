@@ -24,7 +24,10 @@ def ctx():
     c.close()
 
 
-def gpu_burn(ctx, w, solver, max_iter=20000, layout="auto", **kw):
+def gpu_burn(ctx, w, solver, max_iter=20000, layout="auto", normalize=False, **kw):
+    """Burn workload `w` on the GPU; returns (Y, T, dt, status, substeps, iterations) and, with
+    normalize=True (post-burn mass normalisation), the per-particle drift sum_i A_i Y_i - 1 as a
+    seventh entry."""
     import torch
     dev = torch.device("cuda:0")
     ctx.set_layout(layout)
@@ -36,10 +39,22 @@ def gpu_burn(ctx, w, solver, max_iter=20000, layout="auto", **kw):
     st = torch.full((P,), -1, dtype=torch.int32, device=dev)
     it = torch.zeros(P, dtype=torch.int32, device=dev)
     sub = torch.zeros(P, dtype=torch.int32, device=dev)
+    drift = torch.full((P,), np.nan, dtype=torch.float64, device=dev) if normalize else None
     ctx.burn(w["net"], Y, T, rho, dt, w["hydro_dt"], eos=w["eos"], mu=w["mu"], solver=solver, status=st,
-             iterations=it, substeps=sub, max_iter=max_iter, **kw)
+             iterations=it, substeps=sub, max_iter=max_iter, normalize_mass=normalize, mass_drift=drift, **kw)
     torch.cuda.synchronize()
-    return Y.cpu().numpy(), T.cpu().numpy(), dt.cpu().numpy(), st.cpu().numpy(), sub.cpu().numpy(), it.cpu().numpy()
+    out = (Y.cpu().numpy(), T.cpu().numpy(), dt.cpu().numpy(), st.cpu().numpy(), sub.cpu().numpy(),
+           it.cpu().numpy())
+    return out + (drift.cpu().numpy(),) if normalize else out
+
+
+def normalize_mass(net, Y, status):
+    """The post-burn normalisation restated on the host (the oracle side): Y / sum_i A_i Y_i for
+    every particle not skipped; returns (normalised Y, drift sum_i A_i Y_i - 1)."""
+    A = np.asarray(workloads.mass_numbers(net), dtype=np.float64)[: Y.shape[0], None]
+    s = (A * Y).sum(0)
+    burned = status != 1
+    return np.where(burned[None, :], Y / s[None, :], Y), s - 1
 
 
 def binding_energies(net):
@@ -52,13 +67,16 @@ def binding_energies(net):
     return np.array([float(v) for v in body.split(",")])
 
 
-def compare(w, g, o):
-    """Per-particle agreement mask and worst errors (g: gpu tuple, o: oracle tuple)."""
+def compare(w, g, o, burn_Y=None):
+    """Per-particle agreement mask and worst errors (g: gpu tuple, o: oracle tuple).  burn_Y:
+    optional (gpu, oracle) abundances of the burns themselves for the released energy, when g and
+    o hold post-processed (normalised) abundances: the normalisation releases no energy."""
     Yg, Tg, dtg, stg = g[:4]
     Yo, To, dto, sto = o[:4]
     BE = binding_energies(w["net"])[:, None]
-    Eg = (BE * (Yg - w["Y"])).sum(0)
-    Eo = (BE * (Yo - w["Y"])).sum(0)
+    EYg, EYo = burn_Y if burn_Y is not None else (Yg, Yo)
+    Eg = (BE * (EYg - w["Y"])).sum(0)
+    Eo = (BE * (EYo - w["Y"])).sum(0)
     relT = np.abs(Tg - To) / np.abs(To)
     big = Yo > 1e-12
     relY = np.where(big, np.abs(Yg - Yo) / np.where(big, Yo, 1), 0).max(0)
@@ -74,12 +92,36 @@ def compare(w, g, o):
 FLIP_BOUND = 1e-4
 
 
+SUM_X_TOL = 1e-12  # |sum_i X_i - 1| after the post-burn normalisation
+
+
 def check(w, g, o, min_frac=0.95):
     """Statuses must agree for >= 99% of particles (observed: all); >= min_frac of the
     particles must meet the 1e-8 tolerance on T, E and every Y_i > 1e-12 (observed:
     97-100%); the rest are particles whose Newton-stop or accept decision flipped on a
-    rounding-level difference, bounded by FLIP_BOUND in T and in every mass fraction."""
-    ok, relT, relY, relE = compare(w, g, o)
+    rounding-level difference, bounded by FLIP_BOUND in T and in every mass fraction.
+
+    When g carries a seventh entry (the GPU's drift sum_i A_i Y_i - 1 before its post-burn
+    normalisation), g's abundances are normalised: the oracle's are normalised the same way
+    before the comparison, every burned particle of g must have |sum_i X_i - 1| <= SUM_X_TOL,
+    the released energy is compared on the burns' own (un-normalised) states, and the drifts of
+    both sides are reported."""
+    drift_msg = ""
+    burn_Y = None
+    if len(g) > 6:
+        A = np.asarray(workloads.mass_numbers(w["net"]), dtype=np.float64)[: g[0].shape[0], None]
+        burned = g[3] != 1
+        sum_err = np.abs((A * g[0]).sum(0) - 1)[burned]
+        on, od = normalize_mass(w["net"], o[0], o[3])
+        # the burn's own state for the released energy: Y * (1 + drift) on the GPU side (exact to
+        # an ulp), the oracle's output before normalisation
+        burn_Y = (np.where(burned[None, :], g[0] * (1 + g[6])[None, :], g[0]), o[0])
+        o = (on,) + tuple(o[1:])
+        drift_msg = (f"; sum X: max |sum X - 1| after normalisation {sum_err.max() if sum_err.size else 0:.2e}, "
+                     f"drift before: gpu max {np.abs(g[6][burned]).max() if burned.any() else 0:.2e}, "
+                     f"oracle max {np.abs(od[burned]).max() if burned.any() else 0:.2e}")
+        assert sum_err.size == 0 or sum_err.max() <= SUM_X_TOL, drift_msg
+    ok, relT, relY, relE = compare(w, g, o, burn_Y)
     same = g[3] == o[3]
     frac = ok.mean()
     A = np.asarray(workloads.mass_numbers(w["net"]), dtype=np.float64)[: g[0].shape[0], None]
@@ -91,7 +133,8 @@ def check(w, g, o, min_frac=0.95):
            f"max rel within-tolerance T {relT[ok].max() if ok.any() else 0:.2e} "
            f"Y {relY[ok].max() if ok.any() else 0:.2e} E {relE[ok].max() if ok.any() else 0:.2e}; "
            f"flipped: max rel T {relT[flip].max() if flip.any() else 0:.2e}, "
-           f"max |dX| {dX[flip].max() if flip.any() else 0:.2e}, max rel Y {relY[flip].max() if flip.any() else 0:.2e}")
+           f"max |dX| {dX[flip].max() if flip.any() else 0:.2e}, max rel Y {relY[flip].max() if flip.any() else 0:.2e}"
+           + drift_msg)
     print(msg)
     assert same.mean() >= 0.99, msg
     assert frac >= min_frac, msg
@@ -102,8 +145,10 @@ def check(w, g, o, min_frac=0.95):
 @pytest.mark.parametrize("solver", ["dense", "sparse", "mixed"])
 @pytest.mark.parametrize("name,P", [("c1", 4096), ("c2", 512), ("c4", 256)])
 def test_burn_parity(ctx, port, name, P, solver):
+    """Every solver form against the oracle, with the post-burn mass normalisation (sum X = 1
+    to 1e-12, applied identically to the oracle's output)."""
     w = workloads.make(name, P=P, seed=1000 + P)
-    g = gpu_burn(ctx, w, solver)
+    g = gpu_burn(ctx, w, solver, normalize=True)
     o = port.burn(w["net"], w["Y"], w["T"], w["rho"], w["dt"], w["hydro_dt"], w["eos"], w["mu"], max_iter=20000)
     check(w, g, o)
 
@@ -178,12 +223,14 @@ def test_ideal_gas_net86_and_drhodt(ctx, port, solver):
     check(w, g, o)
 
 
-@pytest.mark.parametrize("solver", ["dense", "mixed"])
-def test_golden_fixture_c2(ctx, solver):
-    """GPU against the reference's own outputs (golden fixture of the c2 sample)."""
+@pytest.mark.parametrize("solver", ["dense", "sparse", "mixed"])
+@pytest.mark.parametrize("name", ["c1", "c2", "c4"])
+def test_golden_fixture(ctx, name, solver):
+    """GPU against the reference's own outputs (golden fixtures made by the reference compiled
+    from its sources: tests/golden/gen_golden.py)."""
     from conftest import golden
-    gd = golden("burn_c2.npz")
-    w = workloads.make("c2", P=int(gd["P"]))
+    gd = golden(f"burn_{name}.npz")
+    w = workloads.make(name, P=int(gd["P"]))  # the workload's default seed, as gen_golden.py
     g = gpu_burn(ctx, w, solver)
     check(w, g, (gd["Y"], gd["T"], gd["dt"], gd["status"]))
 
@@ -250,6 +297,30 @@ def test_mixed_network_single_launch(ctx, solver):
         g = gpu_burn(ctx, w, solver)  # same per-particle code as the single launch: bit-identical
         assert np.array_equal(b["Y"].cpu().numpy(), g[0]) and np.array_equal(b["T"].cpu().numpy(), g[1])
         assert np.array_equal(b["status"].cpu().numpy(), g[3])
+
+
+@pytest.mark.parametrize("solver", ["dense", "sparse", "mixed"])
+def test_thread_layout_multi_network_equals_per_network(ctx, solver):
+    """The thread-layout multi-network launch (nnet_burn_batch) equals per-network thread-layout
+    burns bit for bit.  Its mixed form keeps the FP32 factor of every slot in a region above the
+    FP64 rows of all three networks: slots running different networks at the same time must not
+    overlap (an earlier layout put each network's FP32 rows right after its own FP64 rows, where
+    they interleaved with another network's FP64 rows of neighbouring slots)."""
+    import torch
+    dev = torch.device("cuda:0")
+    parts = workloads.make_mixed(4000, 57)
+    one = [dict(network=w["net"], Y=torch.tensor(w["Y"], device=dev), T=torch.tensor(w["T"], device=dev),
+                rho=torch.tensor(w["rho"], device=dev), dt=torch.tensor(w["dt"], device=dev), hydro_dt=w["hydro_dt"],
+                status=torch.zeros(w["T"].size, dtype=torch.int32, device=dev)) for w in parts]
+    ctx.set_layout("thread")
+    ctx.burn_batch(one, solver=solver, max_iter=20000)
+    torch.cuda.synchronize()
+    for w, b in zip(parts, one):
+        g = gpu_burn(ctx, w, solver, layout="thread")
+        assert np.array_equal(b["Y"].cpu().numpy(), g[0]), w["name"]
+        assert np.array_equal(b["T"].cpu().numpy(), g[1]), w["name"]
+        assert np.array_equal(b["status"].cpu().numpy(), g[3]), w["name"]
+    ctx.set_layout("auto")
 
 
 @pytest.mark.parametrize("solver", ["sparse", "mixed"])

@@ -1,13 +1,14 @@
 """nnet_burn_noalloc: the burn for callers that cannot allocate device memory mid-step (codes
 whose device memory all belongs to their own arena allocator, or that cannot afford the
 device-wide synchronisation a cudaMalloc may cause).  Called here through the C ABI with
-ctypes and compared with nnet_burn (the batched layout) on the same inputs, twice in a row,
-because the fixed scratch array keeps the previous call's contents.  The workload holds more
+ctypes and compared bit for bit with nnet_burn (the batched layout) on the same inputs, twice
+in a row, because the fixed scratch array keeps the previous call's contents.  The workload holds more
 particles than the array has slots, so slots are refilled from the work queue.
 
 This file sorts last so that a run stopping at its first failure has run every other test."""
 import ctypes
 
+import numpy as np
 import pytest
 
 import workloads
@@ -77,20 +78,29 @@ def _existing(ctx, w, solver, max_iter=20000):
     return Y.cpu().numpy(), T.cpu().numpy(), dt.cpu().numpy(), st.cpu().numpy()
 
 
+def _same(w, a, b):
+    """nnet_burn_noalloc runs nnet_burn's batched kernel, whose per-particle arithmetic does not
+    depend on the grid: the results must agree bit for bit (Y, T, dt and status); the parity
+    tests' comparison is printed when they do not."""
+    from test_gpu_parity import compare
+    for x, y, name in zip(a, b, ("Y", "T", "dt", "status")):
+        if not np.array_equal(x, y, equal_nan=True):
+            ok = compare(w, a, b)[0]
+            pytest.fail(f"{name} differs from nnet_burn (particles within 1e-8: {int(ok.sum())}/{ok.size})")
+
+
 @pytest.mark.parametrize("solver", ["sparse", "mixed"])
 def test_noalloc_matches_nnet_burn_twice(ctx, solver):
-    from test_gpu_parity import check
     w = workloads.make("c2", P=6000, seed=606)  # more particles than the 4096 fixed slots
     ref = _existing(ctx, w, solver)
-    for _ in range(2):
-        check(w, _noalloc(ctx, w, solver), ref)  # the parity tests' tolerance
+    for _ in range(2):  # the second call finds the first call's contents in the fixed arrays
+        _same(w, _noalloc(ctx, w, solver), ref)
 
 
 def test_noalloc_small_and_rejects_dense(ctx):
     import nnet_gb300 as nn
-    from test_gpu_parity import check
     w = workloads.make("c1", P=40, seed=7)
-    check(w, _noalloc(ctx, w, "sparse"), _existing(ctx, w, "sparse"), min_frac=0.9)
+    _same(w, _noalloc(ctx, w, "sparse"), _existing(ctx, w, "sparse"))
     lib = _lib()
     Y, T, rho, dt, st = _inputs(w)
     a, keep = _args(nn, w, Y, T, rho, dt, st, "dense", 100)

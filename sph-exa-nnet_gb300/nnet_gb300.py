@@ -88,6 +88,9 @@ def burn_args(network, Y, T, rho, dt, hydro_dt, eos=EOS_HELMHOLTZ, mu=0.0, rho_m
         _require_cuda(t, name)
         if t is not None and t.dtype != torch.float64:
             raise NnetError(f"{name} must be float64")
+        # the library reads every array (and every species row of Y) as densely packed
+        if t is not None and t.dim() == 1 and t.numel() > 1 and t.stride(0) != 1:
+            raise NnetError(f"{name} must be contiguous (got stride {t.stride(0)})")
     if order is not None and (order.dtype != torch.int32 or order.numel() != T.numel() or not order.is_cuda):
         raise NnetError("order must be an int32 CUDA tensor of num_particles indices")
     yp = (ctypes.c_void_p * network)(*[r.data_ptr() for r in rows])
@@ -146,6 +149,11 @@ def _ptr(t):
 def _require_cuda(t, name):
     if t is not None and not t.is_cuda:
         raise NnetError(f"{name} must be a CUDA tensor (the library has no CPU path)")
+
+
+def _require_dense(t, name):
+    if t is not None and t.numel() > 1 and not t.is_contiguous():
+        raise NnetError(f"{name} must be contiguous")
 
 
 class Context:
@@ -265,6 +273,10 @@ class Context:
         import torch
         Z = np.ascontiguousarray(Z, dtype=np.float64)
         rows = [Y[j] for j in range(Z.size)]
+        for name, t in [("T", T), ("rho", rho), ("u", u), ("cv", cv), ("p", p), ("c", c), ("dpdT", dpdT)] + [
+                ("Y", r) for r in rows]:
+            _require_cuda(t, name)
+            _require_dense(t, name)
         yp = (ctypes.c_void_p * Z.size)(*[r.data_ptr() for r in rows])
         s = torch.cuda.current_stream(self.device) if stream is None else stream
         _check(_lib.nnet_helmholtz_eos(self.handle, T.numel(), Z.size, Z.ctypes.data_as(ctypes.c_void_p),

@@ -237,6 +237,7 @@ def test_golden_fixture(ctx, name, solver):
 
 def test_edge_cases(ctx):
     import torch
+    import nnet_gb300 as nn
     dev = torch.device("cuda:0")
     w = workloads.make("c1", P=64, seed=9)
     T = w["T"].copy()
@@ -251,8 +252,14 @@ def test_edge_cases(ctx):
     # empty batch is a no-op
     e = torch.zeros(0, dtype=torch.float64, device=dev)
     ctx.burn(14, [e] * 14, e, e, e, 1e-3, eos="ideal", mu=10.0)
+    # abundances in a column-major array: every species row is strided, which the library
+    # cannot read; the host mirror refuses it instead of burning interleaved values
+    Yc = torch.tensor(w["Y"].T.copy(), device=dev).T
+    assert Yc.stride() == (1, 14)
+    Tt, rt, dtt = (torch.tensor(w[k], device=dev) for k in ("T", "rho", "dt"))
+    with pytest.raises(nn.NnetError, match="contiguous"):
+        ctx.burn(14, Yc, Tt, rt, dtt, 1e-3, eos="ideal", mu=10.0)
     # Helmholtz before a table is loaded is an error, not a fault
-    import nnet_gb300 as nn
     c2 = nn.Context(0, helmholtz_table=None)
     with pytest.raises(nn.NnetError):
         c2.burn(86, [e] * 86, e[:0] + torch.ones(1, dtype=torch.float64, device=dev), e, e, 1e-3, eos="helmholtz")

@@ -280,6 +280,14 @@ int nnet_cost_order(nnet_handle h, size_t num_particles, const int32_t* cost, ui
  * scalar work. */
 int nnet_set_batch_slots(nnet_handle h, int slots);
 
+/* Batched layout: rebalance the running particles over the warps once the work queue has
+ * drained (default on; no reference counterpart).  A warp holding more than its share,
+ * ceil(running particles / warps), hands the extra particles to warps holding fewer, each at
+ * its next attempt boundary with everything that attempt depends on, so results are the same
+ * bit for bit; the heaviest particles then run spread over the grid instead of queueing behind
+ * one another in a few warps.  Uses 4 hand-off records (112 bytes each) per slot of the grid. */
+int nnet_set_rebalance(nnet_handle h, int on);
+
 /* Select the particle layout of the sparse and mixed solvers for later nnet_burn calls on
  * `h` (nnet_layout; no reference counterpart: chosen by the autotuner). */
 int nnet_set_layout(nnet_handle h, int layout);

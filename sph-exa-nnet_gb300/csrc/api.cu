@@ -188,6 +188,9 @@ int uploadNetwork(int net, NetBuffer& b)
 
 constexpr int kNetCounters = 16;             // queue head + stats of one launch
 static_assert(1 + kStatWords <= kNetCounters, "counter region too small");
+constexpr int kMigCounterWord = 1 + kStatWords; // the rebalancing counters follow the statistics
+static_assert(kMigCounterWord + 3 <= kNetCounters, "counter region too small");
+constexpr size_t kMigRecordsPerSlot = 4;        // hand-off records reserved per slot of the grid
 constexpr int kCounters    = 4 * kNetCounters; // single launch uses [0, 16); a batch one region per network
 
 int netIndex(int net) { return net == 14 ? 0 : net == 86 ? 1 : net == 87 ? 2 : -1; }
@@ -448,12 +451,26 @@ int nnet_gb300::Workspace::ensureStatus(size_t P, cudaStream_t st)
     return NNET_SUCCESS;
 }
 
+int nnet_gb300::Workspace::ensureMig(size_t cells, cudaStream_t st)
+{
+    if (cells > migCap)
+    {
+        NNET_CUDA(cudaStreamSynchronize(st));
+        if (mig) cudaFree(mig);
+        mig = nullptr, migCap = 0;
+        NNET_CUDA(cudaMalloc(&mig, cells * sizeof(MigCell)));
+        migCap = cells;
+    }
+    return NNET_SUCCESS;
+}
+
 void nnet_gb300::Workspace::release()
 {
     if (scratch) cudaFree(scratch);
     if (counters) cudaFree(counters);
     if (status) cudaFree(status);
-    scratch = nullptr, counters = nullptr, doubles = 0, status = nullptr, statusCap = 0;
+    if (mig) cudaFree(mig);
+    scratch = nullptr, counters = nullptr, doubles = 0, status = nullptr, statusCap = 0, mig = nullptr, migCap = 0;
 }
 
 int nnet_gb300::launchPostBurn(const BurnParams& bp, const NetView& nv, const HelmView& hv, int numSMs,
@@ -587,6 +604,15 @@ int nnet_gb300::launchBurn(nnet_context* h, const nnet_burn_args* a, Workspace& 
         bp.status = ws.status;
     }
 
+    // batched layout: rebalancing of the running particles over the warps once the queue has
+    // drained (not for the server's resumable slices, which rebalance at every slice)
+    if (ki.fusedPost && !rs && sliceIters <= 0 && h->rebalance)
+    {
+        const size_t cells = kMigRecordsPerSlot * slots;
+        if (int rc = ws.ensureMig(cells, st)) return rc;
+        NNET_CUDA(cudaMemsetAsync(ws.mig, 0, cells * sizeof(MigCell), st));
+        bp.migCells = ws.mig, bp.migCap = cells, bp.migCount = ws.counters + kMigCounterWord;
+    }
     NNET_CUDA(cudaMemsetAsync(ws.counters, 0, kCounters * sizeof(unsigned long long), st));
     NetView  nv     = h->nets[ni].view;
     HelmView hv     = h->helm;
@@ -595,6 +621,13 @@ int nnet_gb300::launchBurn(nnet_context* h, const nnet_burn_args* a, Workspace& 
     void*    args[] = {&bp, &nv, &hv, &sc, &stride};
     NNET_CUDA(cudaLaunchKernel(ki.func, dim3((unsigned)blocks), dim3(ki.block), args, ki.smem, st));
     if (postPass) return launchPostBurn(bp, nv, hv, h->numSMs, st);
+    return NNET_SUCCESS;
+}
+
+extern "C" int nnet_set_rebalance(nnet_handle h, int on)
+{
+    if (!h) return fail(NNET_ERR_INVALID, "null handle");
+    h->rebalance = on != 0;
     return NNET_SUCCESS;
 }
 

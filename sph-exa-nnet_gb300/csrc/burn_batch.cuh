@@ -54,6 +54,9 @@ __device__ __forceinline__ int specialSlot(int net, int k)
     return s86[k];
 }
 
+// an empty warp polls for hand-offs at most this often (about 20 us apart) before leaving
+constexpr unsigned kIdlePolls = 1u << 22;
+
 enum : int
 {
     ACT_ACCEPT = 1,  // Y <- clipped candidate
@@ -107,6 +110,7 @@ __device__ bool acquireLane(const BurnParams& bp, const NetView& nv, const HelmV
             s.cycleReset();
         }
         s.nit0 = s.nit;
+        if (bp.migCount) atomicAdd(bp.migCount + 2, 1ull);
         return true;
     }
 }
@@ -118,6 +122,7 @@ __device__ void releaseLane(const BurnParams& bp, const ParticleState& s, int st
     bp.T[p]        = s.T;
     bp.dt[p]       = s.dt;
     atomicAdd(bp.stats + kStatIters, (unsigned long long)(s.nit - s.nit0));
+    if (bp.migCount) atomicAdd(bp.migCount + 2, (unsigned long long)-1ll);
     if (st == kPaused)
     {
         const ResumeState& r = bp.rs;
@@ -162,6 +167,51 @@ __device__ void postWarp(const BurnParams& bp, const NetView& nv, const double (
         ab = warpSum(ab), zb = warpSum(zb);
         if (lane == l) abW = ab, zbW = zb;
     }
+}
+
+// the lowest k set bits of m
+__device__ __forceinline__ unsigned lowestBits(unsigned m, int k)
+{
+    unsigned r = 0;
+    for (; k > 0 && m; --k)
+        r |= m & (0u - m), m &= m - 1;
+    return r;
+}
+
+// Hand this lane's particle over (rebalancing): reserve a record, fill it (published after the
+// warp has written Y back), account its iterations.  Returns the record position or -1.
+__device__ long long donateLane(const BurnParams& bp, const ParticleState& s)
+{
+    if (*(volatile unsigned long long*)bp.migCount >= bp.migCap) return -1;
+    const unsigned long long pos = atomicAdd(bp.migCount, 1ull);
+    if (pos >= bp.migCap) return -1;
+    MigCell& c = bp.migCells[pos];
+    c.p = s.p, c.T = s.T, c.dt = s.dt, c.elapsed = s.elapsed, c.nextT = s.nextT, c.rho = s.rho, c.drho = s.drho;
+    c.nit = s.nit, c.nsub = s.nsub, c.cdPower = s.cdPower, c.cdSteps = s.cdSteps, c.cdDt = s.cdDt, c.cdNt = s.cdNt;
+    atomicAdd(bp.stats + kStatIters, (unsigned long long)(s.nit - s.nit0));
+    atomicAdd(bp.migCount + 2, (unsigned long long)-1ll);
+    return (long long)pos;
+}
+
+// Take the next published hand-off record, if any.  The particle resumes at its attempt
+// boundary: Y is loaded from the particle arrays (past the L1, which may hold lines that
+// predate the donor's write-back).
+__device__ bool takeLane(const BurnParams& bp, ParticleState& s)
+{
+    const unsigned long long h   = *(volatile unsigned long long*)(bp.migCount + 1);
+    const unsigned long long lim = min(*(volatile unsigned long long*)bp.migCount, bp.migCap);
+    if (h >= lim) return false;
+    MigCell& c = bp.migCells[h];
+    if (*(volatile unsigned long long*)&c.seq != h + 1) return false; // reserved, not yet published
+    if (atomicCAS(bp.migCount + 1, h, h + 1) != h) return false;
+    __threadfence();
+    s.p = __ldcg(&c.p), s.T = __ldcg(&c.T), s.dt = __ldcg(&c.dt), s.elapsed = __ldcg(&c.elapsed);
+    s.nextT = __ldcg(&c.nextT), s.rho = __ldcg(&c.rho), s.drho = __ldcg(&c.drho), s.nit = __ldcg(&c.nit);
+    s.nsub = __ldcg(&c.nsub), s.cdPower = __ldcg(&c.cdPower), s.cdSteps = __ldcg(&c.cdSteps);
+    s.cdDt = __ldcg(&c.cdDt), s.cdNt = __ldcg(&c.cdNt);
+    s.i = 1, s.nit0 = s.nit;
+    atomicAdd(bp.migCount + 2, 1ull);
+    return true;
 }
 
 // S2: everything of one Newton iteration that depends on (T, rho) of the slot only
@@ -373,8 +423,55 @@ __device__ void batchLoop(const BurnParams& bp, const NetView& nv, const HelmVie
     double        Tth = 0, rhoT = 0, used = 0, abar = 0, zbar = 0, yElec = 0, xT = 0;
     bool          nanF = false;
 
+    const int    gridWarps = (int)warps;
+    unsigned int idle      = 0; // consecutive iterations without a particle (rebalancing wait)
     for (;;)
     {
+        // ---- rebalancing: once the queue has drained, a warp holding more than its share of
+        //      the running particles hands the extras over at their attempt boundaries, and a
+        //      warp holding fewer takes them; the heaviest particles thus end up spread over the
+        //      grid instead of queueing behind each other in a few warps.  The share is
+        //      ceil(running / warps), at most the warp's slots.
+        long long pubPos = -1;
+        if (bp.migCells)
+        {
+            const unsigned hasM = __ballot_sync(kFull, has);
+            unsigned long long q = 0, enq = 0, deq = 0, run = 0;
+            if (lane == 0)
+            {
+                q   = *(volatile unsigned long long*)bp.queue;
+                enq = *(volatile unsigned long long*)bp.migCount;
+                deq = *(volatile unsigned long long*)(bp.migCount + 1);
+                run = *(volatile unsigned long long*)(bp.migCount + 2);
+            }
+            q = __shfl_sync(kFull, q, 0);
+            if (q >= bp.P)
+            {
+                enq = __shfl_sync(kFull, enq, 0), deq = __shfl_sync(kFull, deq, 0), run = __shfl_sync(kFull, run, 0);
+                const long long total  = (long long)run + (long long)(enq > deq ? enq - deq : 0);
+                const int       share  = (int)min((long long)spw, max(1ll, (total + gridWarps - 1) / gridWarps));
+                const int       n      = __popc(hasM);
+                if (n > share)
+                {
+                    const unsigned cand = __ballot_sync(kFull, has && s.i == 1 && !(act & ACT_LOAD));
+                    if (lowestBits(cand, n - share) >> lane & 1)
+                    {
+                        pubPos = donateLane(bp, s);
+                        if (pubPos >= 0) has = false, act |= ACT_WRITE, pw = s.p; // Y written back in V1
+                    }
+                }
+                else if (n < share && deq < enq)
+                {
+                    const unsigned freeM = ~hasM & (spw >= 32 ? kFull : ((1u << spw) - 1));
+                    for (unsigned m = lowestBits(freeM, share - n); m; m &= m - 1)
+                    {
+                        if (lane == __ffs(m) - 1 && takeLane(bp, s)) has = true, act |= ACT_LOAD;
+                        __syncwarp();
+                    }
+                }
+            }
+        }
+
         // ---- S1: pre-iteration checks (newtonIteration prologue); finished ones are replaced
         bool cont = false;
         while (has)
@@ -446,7 +543,7 @@ __device__ void batchLoop(const BurnParams& bp, const NetView& nv, const HelmVie
                     else
                         bp.Y[j][po] = y;
                 }
-                if (a & ACT_LOAD) y = bp.Y[j][pn];
+                if (a & ACT_LOAD) y = __ldcg(&bp.Y[j][pn]);
                 if (a & ACT_BLEND)
                 {
                     yn = (1 - k::theta) * y + k::theta * (il <= 1 ? y : yn);
@@ -462,6 +559,17 @@ __device__ void batchLoop(const BurnParams& bp, const NetView& nv, const HelmVie
                 // net87: the blended electron abundance Y[86], last element of lane 86 % 32
                 const double ye = __shfl_sync(kFull, ynLast, 86 % 32);
                 if (lane == l) abar = ab, zbar = zb, yElec = NET == 87 ? ye : 0.;
+            }
+        }
+        // publish the hand-off records of this iteration, now that Y is written back
+        if (__any_sync(kFull, pubPos >= 0))
+        {
+            __threadfence();
+            __syncwarp();
+            if (pubPos >= 0)
+            {
+                __threadfence();
+                atomicExch(&bp.migCells[pubPos].seq, (unsigned long long)pubPos + 1);
             }
         }
         // post-burn EOS of the particles finished by this lane (lane-parallel)
@@ -588,7 +696,23 @@ __device__ void batchLoop(const BurnParams& bp, const NetView& nv, const HelmVie
                 if (has) act |= ACT_LOAD;
             }
         }
-        if (!__any_sync(kFull, has || act != 0)) break;
+        if (!__any_sync(kFull, has || act != 0))
+        {
+            // rebalancing: an empty warp stays available while particles are still running, so
+            // that hand-offs find a taker; it waits between polls and gives up after a bound
+            if (!bp.migCells) break;
+            unsigned long long run = 0, pend = 0;
+            if (lane == 0)
+            {
+                run  = *(volatile unsigned long long*)(bp.migCount + 2);
+                pend = *(volatile unsigned long long*)bp.migCount - *(volatile unsigned long long*)(bp.migCount + 1);
+            }
+            run = __shfl_sync(kFull, run, 0), pend = __shfl_sync(kFull, pend, 0);
+            if ((run == 0 && pend == 0) || ++idle > kIdlePolls) break;
+            __nanosleep(pend ? 1000 : 20000);
+            continue;
+        }
+        idle = 0;
     }
 }
 

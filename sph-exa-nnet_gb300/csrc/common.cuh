@@ -141,6 +141,18 @@ struct ResumeState
     unsigned long long *cdDt, *cdNt;
 };
 
+// A particle handed from one warp to another at an attempt boundary (batched layout, after
+// the work queue has drained): everything the next attempt depends on besides Y, which the
+// donor writes back to the particle arrays first.  seq = position + 1 once published.
+struct alignas(16) MigCell
+{
+    unsigned long long seq, p;
+    double             T, dt, elapsed, nextT, rho, drho;
+    long long          nit;
+    int                nsub, cdPower, cdSteps, pad;
+    unsigned long long cdDt, cdNt;
+};
+
 // Batch arguments as seen by the kernels
 struct BurnParams
 {
@@ -176,6 +188,12 @@ struct BurnParams
     const int*          segOf;
     unsigned long long* segFinished;
     int                 laneSlots; // batched layout: particles in flight per warp (0 = 32)
+    // batched layout, optional: rebalancing of the running particles over the warps once the
+    // queue has drained.  migCount: [0] hand-off records reserved, [1] taken, [2] particles
+    // held by warps; migCells: migCap records.
+    MigCell*            migCells;
+    unsigned long long  migCap;
+    unsigned long long* migCount;
 
     __host__ __device__ bool postSteps() const { return normalize || massDrift || eosU; }
 };

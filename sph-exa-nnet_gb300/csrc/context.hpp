@@ -29,8 +29,11 @@ struct Workspace
     unsigned long long* counters = nullptr; // [0] queue head, [1..] stats (BurnParams::stats)
     int32_t*            status    = nullptr; // per-particle statuses when the caller passes none
     size_t              statusCap = 0;       //   and a post-burn pass needs them
+    MigCell*            mig       = nullptr; // hand-off records of the batched layout's rebalancing
+    size_t              migCap    = 0;
     int                 ensure(size_t need, cudaStream_t st);
     int                 ensureStatus(size_t P, cudaStream_t st);
+    int                 ensureMig(size_t cells, cudaStream_t st);
     void                release();
 };
 
@@ -71,6 +74,7 @@ struct nnet_context
     bool                   lastMulti  = false; // last launch was nnet_burn_batch
     int                    layout     = NNET_LAYOUT_AUTO;
     int                    laneSlots  = 32; // batched layout: particles in flight per warp
+    bool                   rebalance  = true; // batched layout: hand particles between warps
     // device addresses of nnet_burn_noalloc's fixed arrays, looked up by its first call on this
     // handle (they live as long as the device context the handle was created in)
     double*                noallocScratch  = nullptr;

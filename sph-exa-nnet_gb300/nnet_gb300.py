@@ -133,6 +133,7 @@ def load_library(path=LIB_PATH):
     lib.nnet_burn_batch.argtypes = [P, ctypes.POINTER(_BurnArgs), I, P]
     lib.nnet_burn_noalloc.argtypes = [P, ctypes.POINTER(_BurnArgs), P]
     lib.nnet_cost_order.argtypes = [P, S, P, P, P]
+    lib.nnet_set_rebalance.argtypes = [P, I]
     _lib = lib
     return lib
 
@@ -175,6 +176,10 @@ class Context:
     def set_layout(self, layout):
         """Particle layout of the sparse / mixed solvers: "auto", "thread", "warp" or "batched"."""
         _check(_lib.nnet_set_layout(self.handle, LAYOUTS[layout] if isinstance(layout, str) else int(layout)))
+
+    def set_rebalance(self, on):
+        """Batched layout: hand running particles between warps once the queue drains (default on)."""
+        _check(_lib.nnet_set_rebalance(self.handle, int(bool(on))))
 
     def set_batch_slots(self, slots):
         """Batched layout: particles in flight per warp (1..32)."""

@@ -187,6 +187,20 @@ def test_warp_layouts_deterministic(ctx, layout):
         assert np.array_equal(x, y)
 
 
+def test_rebalancing_keeps_results(ctx):
+    """Handing running particles between warps after the queue drains (nnet_set_rebalance)
+    changes no particle's arithmetic: with and without it, results are identical bit for bit.
+    More particles than the grid's slots, so the queue drains while heavy ones still run."""
+    w = workloads.make("c2", P=60000, seed=61)
+    ctx.set_rebalance(False)
+    a = gpu_burn(ctx, w, "sparse", layout="batched")
+    ctx.set_rebalance(True)
+    b = gpu_burn(ctx, w, "sparse", layout="batched")
+    ctx.set_layout("auto")
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+
+
 def test_batched_large_c1(ctx, port):
     """More particles than the batched grid holds at once (the queue refills slots)."""
     w = workloads.make("c1", P=40000, seed=41)

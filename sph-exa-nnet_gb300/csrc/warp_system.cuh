@@ -41,28 +41,33 @@ struct WDims
     static constexpr int NNZ = NET == 14 ? kWarpNnzCap14 : kWarpNnzCap86; // factor capacity (checked on host)
 };
 
-// shared-memory layout of one warp (doubles; the float factor of the mixed form overlaps
-// the Jacobian bases `tr`, which are consumed before the solve)
+// Shared-memory layout of one warp (doubles).  Only what the assembly and the solve need at
+// the same time has its own storage: abundances, fluxes and their temperature derivatives,
+// the factor (the right-hand side right after it), and the Jacobian bases `tr`.  The
+// screening potentials and binding energies of the rate evaluation live at the start of the
+// `tr` region (the temperature row takes the binding energies before the fluxes overwrite
+// it); dY/dt, d(dY/dt)/dT and J (Yn - Y) go straight into the right-hand side and the
+// temperature column as they are gathered; the float factor of the mixed form overlaps `tr`,
+// consumed before the solve; the solve vectors reuse the flux storage.  The smaller the
+// system, the more warps an SM holds, and this latency-bound kernel runs faster with each.
 template<int NET, bool MIXED>
 struct WarpSmem
 {
     using D = WDims<NET>;
-    static constexpr int oY = 0, oYn = oY + D::N, oF = oYn + D::N, oDF = oF + D::R, oBE = oDF + D::R,
-                         oA = oBE + D::N, oB = oA + D::NNZ, oDYdt = oB + D::n, oDYdT = oDYdt + D::N,
-                         oJdy = oDYdT + D::N, oTr = oJdy + D::N;
+    static constexpr int kFlux = 2 * D::R > 4 * D::n ? 2 * D::R : 4 * D::n; // f, df; x, r, ipiv, scale
+    static constexpr int oY = 0, oYn = oY + D::N, oF = oYn + D::N, oDF = oF + D::R, oA = oF + kFlux,
+                         oB = oA + D::NNZ, oTr = oB + D::n;
     static constexpr int floatsD = (D::NNZ + 3 * D::n + 1) / 2;
-    static constexpr int doubles = oTr + (MIXED && floatsD > D::NE ? floatsD : D::NE);
+    static constexpr int trD     = D::NE > 2 * D::N ? D::NE : 2 * D::N; // tr; mu and BE before it
+    static constexpr int doubles = oTr + (MIXED && floatsD > trD ? floatsD : trD);
 
-    static_assert(4 * D::n <= 2 * D::R + D::N, "solve vectors must fit the flux storage");
-    double *Y, *Yn, *f, *df, *BE, *A, *b, *dYdt, *mu, *dYdT, *jdy, *tr, *x, *r, *ipiv, *scale;
+    double *Y, *Yn, *f, *df, *BE, *A, *b, *mu, *tr, *x, *r, *ipiv, *scale;
     float * LU, *d, *ipiv32, *x32;
 
     __device__ explicit WarpSmem(double* s)
     {
-        Y = s + oY, Yn = s + oYn, f = s + oF, df = s + oDF, BE = s + oBE, A = s + oA, b = s + oB;
-        dYdt = s + oDYdt, dYdT = s + oDYdT, jdy = s + oJdy, tr = s + oTr;
-        mu = dYdt; // screening potentials live until the rates are done
-        // the solve vectors reuse the flux / binding-energy storage, dead after assembly
+        Y = s + oY, Yn = s + oYn, f = s + oF, df = s + oDF, A = s + oA, b = s + oB, tr = s + oTr;
+        mu = tr, BE = tr + D::N; // rate evaluation only: dead once the fluxes are formed
         x = f, r = f + D::n, ipiv = f + 2 * D::n, scale = f + 3 * D::n;
         LU = reinterpret_cast<float*>(tr), d = LU + D::NNZ, ipiv32 = d + D::n, x32 = ipiv32 + D::n;
     }
@@ -79,6 +84,15 @@ __device__ void warpAssemble(const NetView& nv, WarpSmem<NET, MIXED>& S, double 
     using D                = WDims<NET>;
     const SparseView& sp   = nv.sp;
     const WarpView&   wv   = nv.wv;
+    const double      mtd  = -k::theta * dt;
+    // the factor starts from zero; the temperature row takes -BE / cv (prepareSystemFromGuess,
+    // nuclear_net.hpp:553-556) while the binding energies are still in the `tr` region
+    for (int p = lane; p < sp.nnz; p += 32)
+        S.A[p] = 0.;
+    __syncwarp();
+    for (int i = lane; i < D::N; i += 32)
+        S.A[__ldg(sp.row0Pos + i)] = -S.BE[i] * cvinv;
+    __syncwarp();
     // per-reaction fluxes (dY/dt terms, nuclear_net.hpp:347-381) and Jacobian bases
     // (:395-438), in place of the rates
     for (int q = lane; q < D::R; q += 32)
@@ -110,10 +124,16 @@ __device__ void warpAssemble(const NetView& nv, WarpSmem<NET, MIXED>& S, double 
             S.tr[k] = base > k::epsilonSystem ? tr : 0.;
         }
     }
-    for (int p = lane; p < sp.nnz; p += 32)
-        S.A[p] = 0.;
     __syncwarp();
-    // dY/dt and d(dY/dt)/dT per species
+    // dY/dt and d(dY/dt)/dT per species, straight into the right-hand side (dt dY/dt - theta dt
+    // (Tg - T) d(dY/dt)/dT; the J (Yn - Y) term follows below) and the temperature column
+    // (nuclear_net.hpp:559-579)
+    auto rowT = [&](int s, double dydt, double c0) {
+        double rh = dydt * dt;
+        rh        = rh + mtd * c0 * (Tg - T);
+        S.b[__ldg(sp.iperm + s + 1)] = rh;
+        S.A[__ldg(sp.col0Pos + s)]   = c0 * mtd;
+    };
     for (int t = lane; t < D::N; t += 32)
     {
         const int s = __ldg(wv.sgOrder + t), b0 = __ldg(wv.sgBeg + s), b1 = __ldg(wv.sgBeg + s + 1);
@@ -125,7 +145,7 @@ __device__ void warpAssemble(const NetView& nv, WarpSmem<NET, MIXED>& S, double 
             const int    r = __ldg(wv.sgRx + k);
             a += w * S.f[r], c += w * S.df[r];
         }
-        S.dYdt[s] = a, S.dYdT[s] = c;
+        rowT(s, a, c);
     }
     {
         // the long lists: partial sums of all of them first, then their butterflies interleaved
@@ -147,7 +167,7 @@ __device__ void warpAssemble(const NetView& nv, WarpSmem<NET, MIXED>& S, double 
         if (lane == 0)
 #pragma unroll
             for (int h = 0; h < kMaxHeavy; ++h)
-                if (h < wv.nSgHeavy) S.dYdt[__ldg(wv.sgHeavy + h)] = ha[h], S.dYdT[__ldg(wv.sgHeavy + h)] = hc[h];
+                if (h < wv.nSgHeavy) rowT(__ldg(wv.sgHeavy + h), ha[h], hc[h]);
     }
     // Jacobian entries
     for (int m = lane; m < wv.nJ; m += 32)
@@ -177,7 +197,11 @@ __device__ void warpAssemble(const NetView& nv, WarpSmem<NET, MIXED>& S, double 
                 if (h < wv.nJgHeavy) S.A[__ldg(wv.jPos + __ldg(wv.jgHeavy + h))] = ha[h];
     }
     __syncwarp();
-    // J (Yg - Y) per species row (nuclear_net.hpp:580-589)
+    // J (Yg - Y) per species row, added to the right-hand side (nuclear_net.hpp:580-589)
+    auto addJdy = [&](int i, double jdy) {
+        double& rh = S.b[__ldg(sp.iperm + i + 1)];
+        rh         = rh + mtd * jdy;
+    };
     for (int t = lane; t < D::N; t += 32)
     {
         const int i = __ldg(wv.rjOrder + t), b0 = __ldg(wv.rjBeg + i), b1 = __ldg(wv.rjBeg + i + 1);
@@ -188,7 +212,7 @@ __device__ void warpAssemble(const NetView& nv, WarpSmem<NET, MIXED>& S, double 
             const int m = __ldg(wv.rjEnt + k), j = __ldg(wv.jCol + m);
             a += S.A[__ldg(wv.jPos + m)] * (S.Yn[j] - S.Y[j]);
         }
-        S.jdy[i] = a;
+        addJdy(i, a);
     }
     {
         double ha[kMaxHeavy];
@@ -208,25 +232,14 @@ __device__ void warpAssemble(const NetView& nv, WarpSmem<NET, MIXED>& S, double 
         if (lane == 0)
 #pragma unroll
             for (int h = 0; h < kMaxHeavy; ++h)
-                if (h < wv.nRjHeavy) S.jdy[__ldg(wv.rjHeavy + h)] = ha[h];
+                if (h < wv.nRjHeavy) addJdy(__ldg(wv.rjHeavy + h), ha[h]);
     }
     __syncwarp();
-    // I - theta dt J, the temperature row / column and the right-hand side (:590-608)
-    const double mtd = -k::theta * dt;
+    // I - theta dt J and the temperature entries (:590-608)
     for (int e = lane; e < sp.nsb; e += 32)
     {
         const int p = __ldg(sp.sbPos + e);
         S.A[p]      = __ldg(sp.sbDiag + e) ? 1. - k::theta * dt * S.A[p] : mtd * S.A[p];
-    }
-    for (int i = lane; i < D::N; i += 32)
-    {
-        const double c0 = S.dYdT[i];
-        double       rh = S.dYdt[i] * dt;
-        rh              = rh + mtd * c0 * (Tg - T);
-        rh              = rh + mtd * S.jdy[i];
-        S.b[__ldg(sp.iperm + i + 1)] = rh;
-        S.A[__ldg(sp.col0Pos + i)]   = c0 * mtd;
-        S.A[__ldg(sp.row0Pos + i)]   = -S.BE[i] * cvinv;
     }
     if (lane == 0)
     {

@@ -9,11 +9,14 @@
 //
 // Additions over the reference (identical in the GPU product):
 //  * a per-particle Newton-iteration budget -> status MAXITER;
-//  * exact detection of cycles of the substep loop: between accepted substeps an
+//  * detection of the substep loop's endless retries: between accepted substeps an
 //    attempt is determined by (dt, Newton temperature buffer) alone, and the rejection
 //    rule (nuclear_net.hpp:745-748 together with :899-904) can return to a state it has
-//    seen, after which the reference retries the same attempts forever (period 1 or 2 in
-//    practice); Brent's algorithm on that pair, compared bitwise -> status LIVELOCK;
+//    seen (period 1 or 2 in practice), or settle on the timestep it maps to itself
+//    (dt <- dt 4 / |dT/T| keeps dt where |dT/T| = 4, far above the 0.04 acceptance bound)
+//    and wander there within rounding noise; either way the reference retries forever.
+//    Brent's algorithm on that pair: the Newton temperature compared bitwise, dt equal
+//    within a relative kCycleDtTol -> status LIVELOCK (same rule as the GPU kernels);
 //  * dt == 0 at system build (the reference throws, nuclear_net.hpp:533-549) -> ZERO_DT;
 //  * the Newton temperature buffer starts at 0 (uninitialised in the reference,
 //    nuclear_net.hpp:943 and parallel_nuclear_net.cu:65).
@@ -38,6 +41,8 @@ const double kMinDtStep      = 1e-2;
 const double kNanDtStep      = 2e-1;
 const double kEpsilonSystem  = 1e-40;
 const double kEpsilonVector  = 1e-16;
+// relative dt tolerance of the livelock detection (2^-20)
+const double kCycleDtTol     = 9.5367431640625e-07;
 const double kNRMaxDt        = 1e-2;
 const double kNRDTTarget     = 1e-2;
 const double kNRDTTol        = 4;
@@ -1085,7 +1090,12 @@ struct CycleDetector
     void reset(double dt, double nt) { sdt = bits(dt), snt = bits(nt), power = 1, steps = 0; }
     bool rejected(double dt, double nt)
     {
-        if (bits(dt) == sdt && bits(nt) == snt) return true;
+        if (bits(nt) == snt)
+        {
+            double saved;
+            std::memcpy(&saved, &sdt, sizeof saved);
+            if (bits(dt) == sdt || std::fabs(dt - saved) <= kCycleDtTol * dt) return true;
+        }
         if (++steps == power) sdt = bits(dt), snt = bits(nt), power <<= 1, steps = 0;
         return false;
     }

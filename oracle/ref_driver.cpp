@@ -39,10 +39,12 @@ extern double f[IMAX][JMAX], fd[IMAX][JMAX], ft[IMAX][JMAX], fdd[IMAX][JMAX], ft
 
 namespace
 {
-// Exact cycle detection on the state an attempt starts from.  Between accepted substeps
-// Y, T and the elapsed time do not change, so an attempt is fully determined by
-// (dt, Newton temperature buffer); once that pair repeats, the reference's substep loop
-// replays the same rejected attempts forever.  Brent's algorithm, compared bitwise.
+// Detection of endless retries on the state an attempt starts from.  Between accepted
+// substeps Y, T and the elapsed time do not change, so an attempt is fully determined by
+// (dt, Newton temperature buffer); once that pair repeats, or dt settles (within rounding
+// noise) on the value the rejection rule maps to itself, the reference's substep loop
+// replays rejected attempts forever.  Brent's algorithm, the temperature compared bitwise,
+// dt within a relative 2^-20 (the rule of oracle/nnet_oracle.cpp and of the GPU kernels).
 struct CycleDetector
 {
     unsigned long long sdt = 0, snt = 0;
@@ -56,7 +58,12 @@ struct CycleDetector
     void reset(double dt, double nt) { sdt = bits(dt), snt = bits(nt), power = 1, steps = 0; }
     bool rejected(double dt, double nt)
     {
-        if (bits(dt) == sdt && bits(nt) == snt) return true;
+        if (bits(nt) == snt)
+        {
+            double saved;
+            std::memcpy(&saved, &sdt, sizeof saved);
+            if (bits(dt) == sdt || std::fabs(dt - saved) <= 9.5367431640625e-07 * dt) return true;
+        }
         if (++steps == power) sdt = bits(dt), snt = bits(nt), power <<= 1, steps = 0;
         return false;
     }

@@ -30,6 +30,8 @@ constexpr int    nrMinIt       = 1;
 constexpr int    nrMaxIt       = 11;
 constexpr double nrItTol       = 1e-7;
 constexpr double substepDtTol  = 1e-6;
+// livelock detection: attempt-start timesteps equal within this relative tolerance (2^-20)
+constexpr double cycleDtTol    = 9.5367431640625e-07;
 } // namespace k
 
 // Element e of scratch slot s lives at base[e * stride + s]: a warp touching element e of

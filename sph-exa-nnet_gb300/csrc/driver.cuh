@@ -33,9 +33,13 @@ struct ParticleState
     int                cdPower, cdSteps;
 
     // Between accepted substeps an attempt is fully determined by (dt, Newton temperature
-    // buffer); Brent's algorithm on that pair, compared bitwise, detects the cycles in
-    // which the reference's rejection rule (nuclear_net.hpp:745-748 with :899-904)
-    // retries the same attempts forever.
+    // buffer).  The reference's rejection rule (nuclear_net.hpp:745-748 with :899-904) can
+    // return to a pair it has seen, or let dt settle on the value it maps to itself
+    // (dt <- dt 4 / |dT/T| is stationary where |dT/T| = 4, far above the 0.04 acceptance
+    // bound) and wander there within rounding noise; either way it retries forever.
+    // Brent's algorithm on the pair: the temperature compared bitwise, dt within a relative
+    // kCycleDtTol (a bitwise dt test catches the wandering case only when the noise happens
+    // to repeat a value, after any number of attempts).
     __device__ __forceinline__ void cycleReset()
     {
         cdDt = __double_as_longlong(dt), cdNt = __double_as_longlong(nextT), cdPower = 1, cdSteps = 0;
@@ -43,7 +47,7 @@ struct ParticleState
     __device__ __forceinline__ bool cycleRejected()
     {
         const unsigned long long a = __double_as_longlong(dt), b = __double_as_longlong(nextT);
-        if (a == cdDt && b == cdNt) return true;
+        if (b == cdNt && (a == cdDt || fabs(dt - __longlong_as_double(cdDt)) <= k::cycleDtTol * dt)) return true;
         if (++cdSteps == cdPower) cdDt = a, cdNt = b, cdPower <<= 1, cdSteps = 0;
         return false;
     }

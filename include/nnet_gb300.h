@@ -50,9 +50,10 @@ enum nnet_particle_status
     NNET_PARTICLE_OK       = 0, /* burned to hydro_dt */
     NNET_PARTICLE_SKIPPED  = 1, /* rho <= 1e5 or T <= 1e8: left untouched (parallel_nuclear_net_impl.cpp:83) */
     NNET_PARTICLE_LIVELOCK = 2, /* the substep loop entered a cycle: rejected attempts returned to
-                                   an attempt-start state (dt, Newton temperature) already seen, so
-                                   the reference would retry them forever (nuclear_net.hpp:745-748
-                                   with :899-904); Y and T are those of the last accepted substep */
+                                   an attempt-start state already seen (the same Newton temperature,
+                                   dt equal within a relative 2^-20), so the reference would retry
+                                   them forever (nuclear_net.hpp:745-748 with :899-904); Y and T
+                                   are those of the last accepted substep */
     NNET_PARTICLE_MAXITER  = 3, /* Newton-iteration budget exhausted */
     NNET_PARTICLE_ZERO_DT  = 4, /* timestep underflowed to 0 (the reference throws, nuclear_net.hpp:533-549) */
     NNET_PARTICLE_ABORTED  = 5, /* the launch reached nnet_burn_args.time_limit_seconds (no reference

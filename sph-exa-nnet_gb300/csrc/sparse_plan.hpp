@@ -4,8 +4,8 @@
 // 514-609; index 0 = temperature, 1..N = species) has the structure
 //   row 0 and column 0 dense (energy equation, d(dY/dt)/dT),
 //   species block = identity + the reaction-list Jacobian pattern (:395-438).
-// A greedy minimum-degree ordering on that pattern (ties by index) and a symbolic
-// right-looking elimination give the fill and flat "programs" the kernels execute with
+// A greedy minimum-degree ordering on that pattern (ties by elimination level, then index)
+// and a symbolic right-looking elimination give the fill and flat "programs" the kernels execute with
 // warp-uniform control flow: every particle of a network runs the same operation list
 // on its own values.  For net86 this is 1,044 stored entries and 2,745 multiply-adds
 // per factorisation, against 7,569 entries and about 216k for the dense elimination.

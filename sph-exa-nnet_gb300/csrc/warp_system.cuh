@@ -103,11 +103,10 @@ __device__ void warpAssemble(const NetView& nv, WarpSmem<NET, MIXED>& S, double 
         {
             const int    cnt = __ldg(nv.rcnt + k);
             const double yr  = S.Yn[__ldg(nv.rspec + k)] * rho;
-            if (cnt != 1)
-            {
-                const double fac = cnt == 2 ? 2. : 6.;
-                f /= fac, df /= fac, base /= fac;
-            }
+            if (cnt == 2)
+                f *= 0.5, df *= 0.5, base *= 0.5; // exact: the same value as a division by 2
+            else if (cnt != 1)
+                f /= 6., df /= 6., base /= 6.;
             const double pw = ipowS(yr, cnt);
             f *= pw, df *= pw, base *= ipowS(yr, cnt - 1);
         }
@@ -139,6 +138,9 @@ __device__ void warpAssemble(const NetView& nv, WarpSmem<NET, MIXED>& S, double 
         const int s = __ldg(wv.sgOrder + t), b0 = __ldg(wv.sgBeg + s), b1 = __ldg(wv.sgBeg + s + 1);
         if (b1 - b0 > WarpPlan::kHeavy) continue;
         double a = 0, c = 0;
+        // unrolled gathers (here and below) issue the index and value loads of four entries
+        // before their products are summed, in the same order: latency hidden, same bits
+#pragma unroll 4
         for (int k = b0; k < b1; ++k)
         {
             const double w = __ldg(wv.sgCoef + k);
@@ -175,6 +177,7 @@ __device__ void warpAssemble(const NetView& nv, WarpSmem<NET, MIXED>& S, double 
         const int b0 = __ldg(wv.jgBeg + m), b1 = __ldg(wv.jgBeg + m + 1);
         if (b1 - b0 > WarpPlan::kHeavy) continue;
         double a = 0;
+#pragma unroll 4
         for (int k = b0; k < b1; ++k)
             a += __ldg(wv.jgCoef + k) * S.tr[__ldg(wv.jgEnt + k)];
         S.A[__ldg(wv.jPos + m)] = a;
@@ -207,6 +210,7 @@ __device__ void warpAssemble(const NetView& nv, WarpSmem<NET, MIXED>& S, double 
         const int i = __ldg(wv.rjOrder + t), b0 = __ldg(wv.rjBeg + i), b1 = __ldg(wv.rjBeg + i + 1);
         if (b1 - b0 > WarpPlan::kHeavy) continue;
         double a = 0;
+#pragma unroll 4
         for (int k = b0; k < b1; ++k)
         {
             const int m = __ldg(wv.rjEnt + k), j = __ldg(wv.jCol + m);
@@ -283,6 +287,7 @@ __device__ void levelFactor(const SparseView& sp, const WarpView& wv, F* A, F* i
         {
             const int pos = __ldg(tgPos + t);
             F         a   = A[pos];
+#pragma unroll 4
             for (int u = __ldg(tgUpd + t), ue = __ldg(tgUpd + t + 1); u < ue; ++u)
                 a = a - A[__ldg(tuL + u)] * A[__ldg(tuU + u)];
             A[pos] = a;
@@ -301,6 +306,7 @@ __device__ void levelForward(const WarpView& wv, const F* A, F* y, int lane)
         {
             const int row = __ldg(wv.fwRow + r);
             F         a   = y[row];
+#pragma unroll 4
             for (int e = __ldg(wv.fwEnt + r), ee = __ldg(wv.fwEnt + r + 1); e < ee; ++e)
                 a = a - A[__ldg(wv.flPos + e)] * y[__ldg(wv.flK + e)];
             y[row] = a;
@@ -331,6 +337,7 @@ __device__ void levelBackward(const WarpView& wv, const F* A, const F* ipiv, F* 
             {
                 const int r = r0 + t - nP, row = __ldg(wv.bwRow + r);
                 F         a = y[row];
+#pragma unroll 4
                 for (int e = __ldg(wv.bwEnt + r), ee = __ldg(wv.bwEnt + r + 1); e < ee; ++e)
                 {
                     const int k = __ldg(wv.buK + e);

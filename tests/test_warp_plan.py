@@ -1,8 +1,9 @@
-"""The warp plan on the CPU: for net14, net86 and net87 the level-scheduled LU (reciprocals
-folded into the multiplier round, forward substitution folded into the factorisation,
-one-round backward levels), executed round by round with every lane reading the round's
-starting values, must equal the plain sequential elimination; and the fixed-order gathers
-must reproduce the reaction-list scatters of dY/dt and of the Jacobian."""
+"""The warp plan on the CPU, for net14, net86 and net87: the ordering's level count, fill and
+multiply-adds are pinned; the level-scheduled LU (reciprocals folded into the multiplier
+round, forward substitution folded into the factorisation, one-round backward levels),
+executed round by round with every lane reading the round's starting values, must equal the
+plain sequential elimination; and the fixed-order gathers must reproduce the reaction-list
+scatters of dY/dt and of the Jacobian."""
 import os
 import subprocess
 import tempfile
@@ -30,6 +31,14 @@ int main() {
     WarpPlan W = buildWarpPlan(P, t.rb, t.rs, t.rc, t.pb, t.ps, t.pc, t.cap);
     const int n = P.n, N = P.N;
     if (P.nnz > t.cap) { printf("net%d: factor exceeds capacity\n", t.net); return 1; }
+    // the ordering's figures: minimum degree with ties broken by elimination level (with ties
+    // broken by index, net86 / net87 had the same fill and multiply-adds in 38 levels)
+    const int  expLevels = t.net == 14 ? 13 : 18, expNnz = t.net == 14 ? 98 : t.net == 86 ? 1044 : 1051;
+    const long expFma    = t.net == 14 ? 129 : t.net == 86 ? 2745 : 2754;
+    if (W.nLevels != expLevels || P.nnz != expNnz || P.factorFma != expFma) {
+      printf("net%d: plan has %d levels, %d entries, %lld multiply-adds\n", t.net, W.nLevels, P.nnz, P.factorFma);
+      ++bad;
+    }
     std::mt19937_64 g(5); std::uniform_real_distribution<double> u(0.1, 1);
     std::vector<double> A0(P.nnz), b(n);
     for (auto& v : A0) v = u(g) * 0.01;

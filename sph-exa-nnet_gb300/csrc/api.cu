@@ -130,6 +130,8 @@ int uploadNetwork(int net, NetBuffer& b)
     const WarpPlan wp = buildWarpPlan(sp, rbeg, rspec, rcnt, pbeg, pspec, pcnt, net == 14 ? kWarpNnzCap14 : kWarpNnzCap86);
     if (wp.sgHeavy.size() > 8 || wp.jgHeavy.size() > 8 || wp.rjHeavy.size() > 8 || wp.rowHeavy.size() > 8)
         return fail(NNET_ERR_TOO_LARGE, "network has more long gather lists than the warp kernels unroll");
+    if (wp.rhsBase + sp.n > 0xffff)
+        return fail(NNET_ERR_TOO_LARGE, "factor positions exceed the 16-bit fields of the factorisation ops");
     const size_t oSgC = putd(wp.sgCoef.data(), wp.sgCoef.size()), oJgC = putd(wp.jgCoef.data(), wp.jgCoef.size());
     const size_t oUpdB = putv(wp.updBeg), oUpdT = putv(wp.updT), oUpdL = putv(wp.updL), oUpdU = putv(wp.updU),
                  oUcB = putv(wp.ucBeg), oUcP = putv(wp.ucPos), oUcR = putv(wp.ucRow), oSgB = putv(wp.sgBeg),
@@ -145,6 +147,11 @@ int uploadNetwork(int net, NetBuffer& b)
     const size_t oSgO = putv(wp.sgOrder), oRjO = putv(wp.rjOrder);
     const size_t oScB = putv(wp.scBeg), oScP = putv(wp.scPos), oScK = putv(wp.scPiv), oTgBA = putv(wp.tgBegA),
                  oTgPA = putv(wp.tgPosA), oTgUA = putv(wp.tgUpdA), oTuLA = putv(wp.tuLA), oTuUA = putv(wp.tuUA);
+    const size_t oFoB = putv(wp.foBeg);
+    if (ii.size() % 2) ii.push_back(0); // the 64-bit ops start on an 8-byte boundary
+    const size_t oFOp = ii.size();
+    for (unsigned long long op : wp.fOps)
+        ii.push_back((int)(unsigned)op), ii.push_back((int)(unsigned)(op >> 32)); // little-endian halves
     const size_t bytesD = d.size() * sizeof(double), bytes = bytesD + ii.size() * sizeof(int);
     NNET_CUDA(cudaMalloc(&b.mem, bytes));
     NNET_CUDA(cudaMemcpy(b.mem, d.data(), bytesD, cudaMemcpyHostToDevice));
@@ -183,6 +190,7 @@ int uploadNetwork(int net, NetBuffer& b)
     x.rhsBase = wp.rhsBase;
     x.scBeg = I + oScB, x.scPos = I + oScP, x.scPiv = I + oScK, x.tgBegA = I + oTgBA, x.tgPosA = I + oTgPA;
     x.tgUpdA = I + oTgUA, x.tuLA = I + oTuLA, x.tuUA = I + oTuUA;
+    x.fOps = reinterpret_cast<const unsigned long long*>(I + oFOp), x.foBeg = I + oFoB;
     return NNET_SUCCESS;
 }
 

@@ -67,9 +67,12 @@ struct WarpView
     const int *lvBeg, *lvPiv, *lsBeg, *lsPos, *lsPiv, *tgBeg, *tgPos, *tgUpd, *tuL, *tuU;
     const int *fwBeg, *fwRow, *fwEnt, *flPos, *flK, *bwBeg, *bwRow, *bwEnt, *buPos, *buK;
     const int *sgOrder, *rjOrder;
-    // fused forms (WarpPlan::scBeg ... tuUA)
-    int        rhsBase;
-    const int *scBeg, *scPos, *scPiv, *tgBegA, *tgPosA, *tgUpdA, *tuLA, *tuUA;
+    // fused forms (WarpPlan::scBeg ... tuUA), and the fused factorisation's per-lane op
+    // streams (WarpPlan::fOps, foBeg)
+    int                       rhsBase;
+    const int *               scBeg, *scPos, *scPiv, *tgBegA, *tgPosA, *tgUpdA, *tuLA, *tuUA;
+    const unsigned long long* fOps;
+    const int*                foBeg;
 };
 
 // Read-only device view of one network definition (reaction list in CSR form, binding

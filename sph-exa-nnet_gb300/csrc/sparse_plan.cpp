@@ -257,6 +257,29 @@ void buildLevels(const SparsePlan& P, WarpPlan& W, int rhsBase)
         W.scBeg.push_back((int)W.scPos.size());
         W.tgBegA.push_back((int)W.tgPosA.size());
     }
+    // the same updates as one stream of ops per lane and level: the level's targets (longest
+    // list first) each go to the lane with the fewest updates so far, so a level takes as many
+    // rounds as its busiest lane has updates, instead of the sum over its rounds of 32 targets
+    // of their longest list; a target keeps its updates in pivot order on one lane.
+    W.foBeg = {0};
+    for (int l = 0; l < nl; ++l)
+    {
+        std::vector<std::vector<unsigned long long>> lane(32);
+        std::vector<int>                             load(32, 0);
+        for (int t = W.tgBegA[l]; t < W.tgBegA[l + 1]; ++t)
+        {
+            const int q  = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+            const int u0 = W.tgUpdA[t], u1 = W.tgUpdA[t + 1];
+            for (int u = u0; u < u1; ++u)
+                lane[q].push_back(WarpPlan::factorOp(W.tuLA[u], W.tuUA[u], W.tgPosA[t], u == u0, u == u1 - 1));
+            load[q] += u1 - u0;
+        }
+        const int rows = *std::max_element(load.begin(), load.end());
+        for (int k = 0; k < rows; ++k)
+            for (int q = 0; q < 32; ++q)
+                W.fOps.push_back(k < (int)lane[q].size() ? lane[q][k] : 0ull);
+        W.foBeg.push_back(W.foBeg.back() + rows);
+    }
     // backward: levels last to first; rows above the level's pivots, by U column
     W.bwBeg = {0}, W.bwEnt = {0};
     for (int l = nl - 1; l >= 0; --l)

@@ -98,6 +98,18 @@ struct WarpPlan
     //   level's targets including the right-hand-side rows.
     int              rhsBase = 0;
     std::vector<int> scBeg, scPos, scPiv, tgBegA, tgPosA, tgUpdA, tuLA, tuUA;
+    // The fused factorisation's updates as per-lane op streams: level l takes rows
+    // foBeg[l] .. foBeg[l+1] of fOps, 32 ops per row (op k of lane q at row k, column q).  An
+    // op is target -= A[L] * A[U]; it loads the target first when it is the target's first,
+    // stores it when it is the last; 0 is no op (see factorOp).
+    std::vector<unsigned long long> fOps;
+    std::vector<int>                foBeg;
+    static constexpr unsigned long long kOpFirst = 1ull << 48, kOpLast = 1ull << 49, kOpValid = 1ull << 50;
+    static unsigned long long factorOp(int L, int U, int target, bool first, bool last)
+    {
+        return (unsigned long long)L | (unsigned long long)U << 16 | (unsigned long long)target << 32 |
+               (first ? kOpFirst : 0) | (last ? kOpLast : 0) | kOpValid;
+    }
 };
 
 // capacity of the factor storage of the warp-cooperative kernels (the right-hand side

@@ -283,15 +283,36 @@ __device__ void levelFactor(const SparseView& sp, const WarpView& wv, F* A, F* i
             ipiv[k] = ip; // lanes of one pivot write the same value
         }
         __syncwarp();
-        for (int t = __ldg(tgBeg + l) + lane; t < __ldg(tgBeg + l + 1); t += 32)
+        if constexpr (AUG)
         {
-            const int pos = __ldg(tgPos + t);
-            F         a   = A[pos];
+            // the level's updates as this lane's op stream (WarpPlan::fOps): the same products
+            // per target in the same order as the target lists below, packed onto the lanes
+            const int                 r0 = __ldg(wv.foBeg + l), nr = __ldg(wv.foBeg + l + 1) - r0;
+            const unsigned long long* op = wv.fOps + (size_t)r0 * 32 + lane;
+            F                         a  = 0;
 #pragma unroll 4
-            for (int u = __ldg(tgUpd + t), ue = __ldg(tgUpd + t + 1); u < ue; ++u)
-                a = a - A[__ldg(tuL + u)] * A[__ldg(tuU + u)];
-            A[pos] = a;
+            for (int k = 0; k < nr; ++k)
+            {
+                const unsigned long long o = __ldg(op + (size_t)k * 32);
+                if (o & WarpPlan::kOpValid)
+                {
+                    const int pos = (int)(o >> 32) & 0xffff;
+                    if (o & WarpPlan::kOpFirst) a = A[pos];
+                    a = a - A[(int)o & 0xffff] * A[(int)(o >> 16) & 0xffff];
+                    if (o & WarpPlan::kOpLast) A[pos] = a;
+                }
+            }
         }
+        else
+            for (int t = __ldg(tgBeg + l) + lane; t < __ldg(tgBeg + l + 1); t += 32)
+            {
+                const int pos = __ldg(tgPos + t);
+                F         a   = A[pos];
+#pragma unroll 4
+                for (int u = __ldg(tgUpd + t), ue = __ldg(tgUpd + t + 1); u < ue; ++u)
+                    a = a - A[__ldg(tuL + u)] * A[__ldg(tuU + u)];
+                A[pos] = a;
+            }
         __syncwarp();
     }
 }

@@ -112,7 +112,39 @@ int main() {
     for (int s : W.sgOrder) seenS[s]++;
     for (int i : W.rjOrder) seenR[i]++;
     for (int i = 0; i < N; ++i) bad += seenS[i] != 1 || seenR[i] != 1;
-    printf("net%d levels %d solve %.2e gathers %.2e %.2e\n", t.net, W.nLevels, dx, dsg, dj);
+    // the per-lane op streams of the fused factorisation carry, for every target of a level,
+    // exactly its update list in order, on one lane, contiguously
+    long opRows = 0;
+    for (int l = 0; l < W.nLevels; ++l) {
+      const int rows = W.foBeg[l + 1] - W.foBeg[l];
+      opRows += rows;
+      std::vector<int> seen(W.tgBegA[l + 1] - W.tgBegA[l], 0);
+      int busiest = 0;
+      for (int q = 0; q < 32; ++q) {
+        int cur = -1, next = 0, used = 0;
+        for (int k = 0; k < rows; ++k) {
+          const unsigned long long o = W.fOps[(size_t)(W.foBeg[l] + k) * 32 + q];
+          if (!(o & WarpPlan::kOpValid)) { bad += cur >= 0; cur = -2; continue; }
+          bad += cur == -2;  // no op before the end of a lane's stream
+          ++used;
+          const int L = o & 0xffff, U = (o >> 16) & 0xffff, pos = (o >> 32) & 0xffff;
+          if (o & WarpPlan::kOpFirst) {
+            bad += cur >= 0;
+            cur = -1;
+            for (int t2 = W.tgBegA[l]; t2 < W.tgBegA[l + 1]; ++t2) if (W.tgPosA[t2] == pos) cur = t2;
+            if (cur < 0) { ++bad; break; }
+            seen[cur - W.tgBegA[l]]++, next = W.tgUpdA[cur];
+          }
+          if (cur < 0 || next >= W.tgUpdA[cur + 1] || W.tuLA[next] != L || W.tuUA[next] != U || W.tgPosA[cur] != pos) { ++bad; break; }
+          ++next;
+          if (o & WarpPlan::kOpLast) { bad += next != W.tgUpdA[cur + 1]; cur = -1; }
+        }
+        busiest = busiest > used ? busiest : used;
+      }
+      for (int v : seen) bad += v != 1;
+      bad += busiest != rows;
+    }
+    printf("net%d levels %d op rows %ld solve %.2e gathers %.2e %.2e\n", t.net, W.nLevels, opRows, dx, dsg, dj);
     bad += !(dx < 1e-13 && dsg < 1e-14 && dj < 1e-14);
   }
   return bad;

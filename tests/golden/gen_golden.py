@@ -10,8 +10,14 @@ these fixtures are its outputs on:
   burn_*.npz     batch burns of seeded samples of the c1 / c2 / c4 workloads
   nr_net14.npz   a solveSystemNR trajectory like test/net14_test.cpp:134-187
                  (C-O burning, rho=1e9, T=1e9, ideal gas mu=10)
+  burn_special.npz  single particles whose substep loop never ends in the reference (see
+                 SPECIAL): one whose timestep wanders at the rejection rule's fixed point
+                 (LIVELOCK once attempt-start timesteps repeat within 2^-20), one whose
+                 rejections follow a chaotic timestep map and one alternating between two
+                 timesteps from a wandering Newton temperature buffer (both MAXITER)
 
-usage: python tests/golden/gen_golden.py
+usage: python tests/golden/gen_golden.py            (all fixtures)
+       python tests/golden/gen_golden.py special    (burn_special.npz only)
 """
 import os
 import sys
@@ -29,12 +35,36 @@ import workloads  # noqa: E402
 from oracle import Oracle  # noqa: E402
 
 BURN_CASES = {"c1": 1024, "c2": 192, "c4": 96}
+# (workload, network of a c3 part or None, particle index in it, Newton-iteration budget)
+SPECIAL = [("c2", None, 168389, 20000), ("c3", 86, 881263, 2000), ("c3", 14, 169533, 2000)]
+
+
+def special(ref):
+    """burn_special.npz: the reference's burns of the SPECIAL particles."""
+    out = {}
+    for k, (name, net, i, budget) in enumerate(SPECIAL):
+        w = workloads.make(name)
+        if net is not None:
+            w = [p for p in w if p["net"] == net][0]
+        Y0, T0, rho, dt0 = (np.ascontiguousarray(w[f][..., i:i + 1]) for f in ("Y", "T", "rho", "dt"))
+        Y, T, dt, st, sub, it = ref.burn(w["net"], Y0, T0, rho, dt0, w["hydro_dt"], w["eos"], w["mu"],
+                                         max_iter=budget)
+        out.update({f"{k}_net": w["net"], f"{k}_eos": w["eos"], f"{k}_mu": w["mu"], f"{k}_hydro_dt": w["hydro_dt"],
+                    f"{k}_budget": budget, f"{k}_Y0": Y0, f"{k}_T0": T0, f"{k}_rho": rho, f"{k}_dt0": dt0,
+                    f"{k}_Y": Y, f"{k}_T": T, f"{k}_dt": dt, f"{k}_status": st, f"{k}_substeps": sub,
+                    f"{k}_iters": it})
+        print(name, net, i, "status", int(st[0]), "iterations", int(it[0]))
+        del w
+    np.savez_compressed(os.path.join(HERE, "burn_special.npz"), cases=len(SPECIAL), **out)
 
 
 def main():
     ref = Oracle("ref")
     tab = np.stack([gen_helm_table.tables()[n] for n in gen_helm_table.NAMES]).reshape(-1)
     ref.load_helmholtz(tab)
+    special(ref)
+    if sys.argv[1:] == ["special"]:
+        return
 
     # ---- rate known-answer tests
     out = {}

@@ -54,6 +54,31 @@ def test_burn_golden(port, name):
     assert close(T, g["T"]) and close(dt, g["dt"]) and close(Y, g["Y"])
 
 
+def test_never_ending_particles(port):
+    """Three particles on which the reference's substep loop never ends (burn_special.npz, made
+    from the reference build): the c2 particle whose timestep wanders at the rejection rule's
+    fixed point ends LIVELOCK within a few dozen Newton iterations (attempt-start timesteps
+    equal within 2^-20; bitwise detection needed thousands or never closed it); the c3 particles
+    whose rejections never repeat run their whole budget and end MAXITER.  All keep the state of
+    their last accepted substep, as the reference does."""
+    g = golden("burn_special.npz")
+    want = [(2, 100), (3, None), (3, None)]
+    for k in range(int(g["cases"])):
+        c = lambda f: g[f"{k}_{f}"]
+        Y, T, dt, st, sub, it = port.burn(int(c("net")), c("Y0"), c("T0"), c("rho"), c("dt0"), float(c("hydro_dt")),
+                                          str(c("eos")), float(c("mu")), max_iter=int(c("budget")))
+        assert np.array_equal(st, c("status")) and np.array_equal(sub, c("substeps")), k
+        assert np.array_equal(it, c("iters")), k
+        assert close(T, c("T")) and close(dt, c("dt")) and close(Y, c("Y")), k
+        status, most = want[k]
+        assert st[0] == status, k
+        if most is not None:
+            assert it[0] <= most, k
+        else:
+            assert it[0] == int(c("budget")) and sub[0] == 0, k
+            assert np.array_equal(Y, c("Y0")) and np.array_equal(T, c("T0")), k
+
+
 def test_solve_nr_trajectory(port):
     traj = golden("nr_net14.npz")["traj"]
     Y = workloads.composition(14, 1, 0.5, 0.5, 0.0)[:, 0]

@@ -255,8 +255,7 @@ __device__ void warpAssemble(const NetView& nv, WarpSmem<NET, MIXED>& S, double 
 }
 
 // ------------------------------------------------------------------ solves (warp)
-// Level-scheduled right-looking LU without pivoting, in place (FP64 or FP32): per level,
-// the pivots' reciprocals, then their multipliers, then every target's updates in pivot order.
+// pivot reciprocals, rounded to nearest
 __device__ __forceinline__ double recip(double a) { return __drcp_rn(a); }
 __device__ __forceinline__ float  recip(float a) { return __frcp_rn(a); }
 
@@ -264,7 +263,8 @@ __device__ __forceinline__ float  recip(float a) { return __frcp_rn(a); }
 // the multipliers (each lane forms its pivot's reciprocal itself, so no separate round is
 // needed), then every target's updates in pivot order.  AUG: the right-hand side, stored
 // right after the factor's rhsBase entries, is a column of the matrix, so the forward
-// substitution happens in the same rounds.
+// substitution happens in the same rounds; the updates then run as per-lane op streams
+// (WarpPlan::fOps), the other form as rounds of 32 targets.
 template<typename F, bool AUG>
 __device__ void levelFactor(const SparseView& sp, const WarpView& wv, F* A, F* ipiv, int lane)
 {
